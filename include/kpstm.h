@@ -1,0 +1,213 @@
+/*
+ * kpstm.h - C ABI of the GB300 Kirchhoff prestack time migration.
+ *
+ * Drop-in boundary for the reference's imaging job
+ *     void kirchhoff(int job_id)                       Kirchhoff.c:92, 1104-1616
+ * and the set-up it depends on (count_size_file Kirchhoff.c:633-722,
+ * create_aliasfilter :380-441, build_vel_model :447-626, the image/slab
+ * arithmetic of main :266-313).  The reference passes everything through
+ * globals and compile-time #defines (Kirchhoff.c:17-65); here the same
+ * quantities travel in kpstm_params / kpstm_velocity, and the file reads and
+ * writes of kirchhoff() become buffer arguments:
+ *
+ *   reference (Kirchhoff.c)                      this ABI
+ *   -------------------------------------------  ------------------------------
+ *   main: sinA/cosA, Nx/Ny, nx/ny, slabs :266-313  kpstm_create
+ *   create_aliasfilter :380-441                    kpstm_create (and
+ *                                                  kpstm_aliasfilter, stand-alone)
+ *   build_vel_model :447-626 (v_rms grid, v^2)     kpstm_velocity + kpstm_create
+ *   kirchhoff: one ntblock iteration :1276-1408    kpstm_add_traces /
+ *     (fread + IBM decode :1280-1290,              kpstm_add_segy_block /
+ *      geometry :1297-1310, imaging :1312-1403)    kpstm_add_traces_device
+ *   kirchhoff: finishing :1426-1479                kpstm_finish
+ *   kirchhoff: SU writer :1482-1593                kpstm_write_su
+ *
+ * Conventions (the reference prints and calls exit(1) on every error; this
+ * ABI never exits and never prints):
+ *   - every call returns a kpstm_status; kpstm_strerror() names it;
+ *   - the caller owns every host buffer it passes; a context owns its device
+ *     buffers and its CUDA stream; all device work of a context is ordered on
+ *     that stream;
+ *   - one context per host thread; contexts are independent.
+ */
+#ifndef KPSTM_H
+#define KPSTM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KPSTM_ABI_VERSION 1
+
+typedef enum {
+    KPSTM_OK = 0,
+    KPSTM_ERR_INVALID_ARG = 1,     /* NULL pointer, size <= 0, inconsistent parameters */
+    KPSTM_ERR_CUDA = 2,            /* a CUDA runtime call failed */
+    KPSTM_ERR_OUT_OF_MEMORY = 3,   /* host or device allocation failed */
+    KPSTM_ERR_VELOCITY_ZERO = 4,   /* a v_rms sample is 0 (Kirchhoff.c:614-615 reports it) */
+    KPSTM_ERR_VELOCITY_RANGE = 5,  /* an image column maps below the velocity grid origin:
+                                      Kirchhoff.c:1357-1365 clamps only the upper end */
+    KPSTM_ERR_GEOMETRY = 6,        /* header coordinate minus origin does not fit an int */
+    KPSTM_ERR_STATE = 7,           /* call out of order (e.g. traces after finish) */
+    KPSTM_ERR_TIMEOUT = 8,         /* a bounded device-side wait gave up */
+    KPSTM_ERR_NO_DEVICE = 9,       /* no CUDA device visible */
+    KPSTM_ERR_SEGY = 10,           /* malformed SEG-Y buffer */
+    KPSTM_ERR_UNSUPPORTED = 11,    /* valid request this build does not implement */
+    KPSTM_ERR_TRANGE = 12          /* trangeMax < 2: the reference's triangle taps
+                                      (Kirchhoff.c:1391-1392) would read before the trace */
+} kpstm_status;
+
+/* Imaging operator. */
+typedef enum {
+    KPSTM_MODE_REFERENCE = 0,  /* Kirchhoff.c:1341-1403 bit for bit: nearest-sample
+                                  T, fixed [P(T+2) - 2P(T) + P(T-2)] triangle, unit weight */
+    KPSTM_MODE_FULL = 1        /* linear trace interpolation, obliquity and spreading
+                                  weight, variable-width triangle anti-alias */
+} kpstm_mode;
+
+/* Trace storage / image accumulation. */
+typedef enum {
+    KPSTM_PREC_FP32 = 0,       /* fp32 traces, fp32 image accumulators */
+    KPSTM_PREC_BF16_KAHAN = 1  /* bf16 traces with a per-trace fp32 scale, fp32
+                                  Kahan-compensated image accumulators */
+} kpstm_precision;
+
+/* Output layout. */
+typedef enum {
+    KPSTM_OUT_OFFSET_GATHERS = 0, /* [nx][ny][nh][ns], as Kirchhoff.c:1438-1445 writes */
+    KPSTM_OUT_STACK = 1           /* [nx][ny][ns]: all offset classes in one image */
+} kpstm_output;
+
+/* Everything kirchhoff() reads from globals and #defines. */
+typedef struct {
+    /* trace sampling, count_size_file (Kirchhoff.c:655-661) */
+    int32_t ns;
+    float dt;                       /* seconds (header microseconds / 1e6) */
+    /* image box in line numbers (Kirchhoff.c:34-37) and increments (:40-41) */
+    int32_t start_iline, end_iline, start_xline, end_xline;
+    double inc_iline, inc_xline;
+    /* physical line spacing (Kirchhoff.c:54-55) */
+    double iline_distance, xline_distance;
+    /* offset classes (Kirchhoff.c:44-46): class = floor((2*sqrt(h^2) - oh)/dh) */
+    int32_t nh;
+    double oh, dh;
+    /* survey origin and rotation (Kirchhoff.c:49-51) */
+    double ox, oy, angle_e_to_n_deg;
+    /* 1.0: coordinates used as in Kirchhoff.c:1297-1304.  Any other value:
+       coordinates scaled as in Kirchhoff_GHTest1.c:56, 1302-1312. */
+    double xy_scale;
+    /* aperture (Kirchhoff.c:58) in coordinate units; low-pass cutoff in Hz (:59) */
+    double aperture, anti_alias_cutoff;
+    /* image slab grid and the slab this context images (Kirchhoff.c:64-65,
+       280-300, 1104): jobs_x * jobs_y slabs, job_id in [0, jobs_x*jobs_y) */
+    int32_t jobs_x, jobs_y, job_id;
+    int32_t mode;       /* kpstm_mode */
+    int32_t precision;  /* kpstm_precision */
+    int32_t output;     /* kpstm_output */
+    /* KPSTM_MODE_FULL only: largest triangle half-width in samples (0 = trangeMax) */
+    int32_t aa_max_halfwidth;
+    int32_t reserved[7];
+} kpstm_params;
+
+/* Gridded v_rms model, build_vel_model (Kirchhoff.c:22-27, 447-626).  Values
+   are v_rms (not squared; the library squares them as Kirchhoff.c:617 does),
+   laid out [n_iline][n_xline][nsm].  Grid line (i, j) holds the trace whose
+   headers carry iline = o_iline + i*d_iline, xline = o_xline + j*d_xline. */
+typedef struct {
+    int32_t n_iline, n_xline, nsm;
+    int32_t o_iline, o_xline, d_iline, d_xline;
+    float dtm;                      /* seconds */
+    const float *vrms;              /* host pointer, read during kpstm_create only */
+} kpstm_velocity;
+
+/* Sizes of the image slab a context produces. */
+typedef struct {
+    int32_t Nx, Ny;          /* whole image, Kirchhoff.c:266-277 */
+    int32_t nx, ny;          /* this slab, Kirchhoff.c:280-281, 295-298 */
+    int32_t nh, ns;          /* classes (1 for a stack), samples */
+    int32_t trange_max;      /* Kirchhoff.c:394 */
+    int32_t x0, y0;          /* first column of the slab: xslice*nx, yslice*ny */
+    int64_t out_elems;       /* floats kpstm_finish writes */
+} kpstm_dims;
+
+typedef struct kpstm_ctx kpstm_ctx;
+
+/* Set-up (= main :263-331 for one job).  Uploads the velocity model and the
+   per-column tables; allocates the slab's image accumulators. */
+int kpstm_create(const kpstm_params *params, const kpstm_velocity *vel, kpstm_ctx **out);
+void kpstm_destroy(kpstm_ctx *ctx);
+int kpstm_get_dims(const kpstm_ctx *ctx, kpstm_dims *dims);
+/* Zero the image accumulators (start a new job with the same set-up). */
+int kpstm_reset(kpstm_ctx *ctx);
+
+/* One ntblock iteration of Kirchhoff.c:1276-1408 from host buffers.
+   hdr_be:  [ntr][60] SEG-Y trace-header words exactly as read from the file
+            (big-endian); words 18-21 (sx, sy, gx, gy) are used.
+   samples: [ntr][ns] IEEE float samples in host byte order (already decoded).
+   Traces are imaged in the order given, as the reference does. */
+int kpstm_add_traces(kpstm_ctx *ctx, const int32_t *hdr_be, const float *samples, int64_t ntr);
+
+/* Same, from a raw SEG-Y trace block: ntr records of 240 header bytes plus
+   ns big-endian IBM floats (the buffer Kirchhoff.c:1280-1281 freads).  The
+   IBM decode of Kirchhoff.c:1284-1290 runs on the device. */
+int kpstm_add_segy_block(kpstm_ctx *ctx, const void *segy_records, int64_t ntr);
+
+/* Same, with headers and samples already in device memory (no host copies).
+   d_hdr_be: [ntr][60] big-endian words; d_samples: [ntr][ns] floats. */
+int kpstm_add_traces_device(kpstm_ctx *ctx, const int32_t *d_hdr_be, const float *d_samples,
+                            int64_t ntr);
+
+/* Finishing, Kirchhoff.c:1426-1479: derivative with -t*dt^2/fold scaling,
+   low-pass by the anti-alias spectrum, first sample zeroed.  out receives
+   dims.out_elems floats in [nx][ny][nh][ns] order (stack: [nx][ny][ns]);
+   fold (nullable) receives the fold counts (1 + contributing traces) in the
+   same layout.  Host pointers.  The accumulators are left untouched, so more
+   traces may follow. */
+int kpstm_finish(kpstm_ctx *ctx, float *out, float *fold);
+/* Same, into device memory. */
+int kpstm_finish_device(kpstm_ctx *ctx, float *d_out, float *d_fold);
+
+/* Raw accumulators before finishing (km_data and fold of Kirchhoff.c:1263-1274),
+   [nx][ny][nh][ns] (stack: [nx][ny][ns]); host pointers, either nullable. */
+int kpstm_get_accumulators(kpstm_ctx *ctx, float *km, float *fold);
+
+/* Number of (trace, in-aperture column, sample) pairs imaged so far. */
+int kpstm_pair_count(const kpstm_ctx *ctx, int64_t *pairs);
+
+/* Device synchronisation of the context's stream. */
+int kpstm_synchronize(kpstm_ctx *ctx);
+
+/* ---- stand-alone set-up helpers (host only) -------------------------------- */
+
+/* create_aliasfilter, Kirchhoff.c:380-441: trangeMax and the low-pass
+   spectrum anti_alias[ns] (including the reference's mirror of the upper
+   half, which zeroes bins ns/2 and ns/2+1 for odd ns). */
+int kpstm_aliasfilter(int32_t ns, float dt, double iline_distance, double xline_distance,
+                      double anti_alias_cutoff, int32_t *trange_max, float *anti_alias);
+
+/* IBM System/360 single precision (big-endian words) to IEEE float, exactly
+   as Kirchhoff.c:1284-1290 computes it. */
+int kpstm_ibm_to_ieee(const uint32_t *ibm_be, float *out, int64_t n);
+
+/* Sampling of a SEG-Y file image in memory, count_size_file
+   (Kirchhoff.c:650-661): ns and dt from the first trace header, number of
+   traces from the size. */
+int kpstm_segy_info(const void *file_bytes, int64_t nbytes, int32_t *ns, float *dt,
+                    int64_t *ntraces);
+
+/* SU trace records of a finished image, Kirchhoff.c:1482-1593: 240-byte
+   big-endian header plus ns big-endian floats per output trace, traces in
+   xc, yc, class order.  dst must hold dims.nx*dims.ny*nh*(240+4*ns) bytes. */
+int kpstm_write_su(const kpstm_ctx *ctx, const float *image, void *dst, int64_t dst_bytes);
+
+const char *kpstm_strerror(int status);
+int kpstm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KPSTM_H */

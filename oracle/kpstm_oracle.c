@@ -1,0 +1,321 @@
+/*
+ * CPU oracle for the Kirchhoff PSTM path - TEST INFRASTRUCTURE ONLY.
+ * See kpstm_oracle.h for the role of this file and how it is pinned to the
+ * compiled reference.  Every function cites the reference lines it restates.
+ *
+ * Build: gcc -O2 -ffp-contract=off (no FMA contraction, which aarch64 gcc
+ * would otherwise apply to float expressions such as cosA*i + sinA*j).
+ */
+#include "kpstm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#include "shim/fftw3.h"
+
+#define KO_PI 3.14159265359 /* Kirchhoff.c:96 */
+
+static uint32_t be32(int32_t w)
+{
+    uint32_t u = (uint32_t)w;
+    return (u >> 24) | ((u >> 8) & 0xFF00u) | ((u << 8) & 0xFF0000u) | (u << 24);
+}
+
+/* main(), Kirchhoff.c:266-313. */
+int ko_dims_of(const kpstm_params *p, ko_dims *d)
+{
+    if (!p || !d || p->ns <= 0 || !(p->dt > 0) || p->jobs_x <= 0 || p->jobs_y <= 0 || p->nh <= 0)
+        return KPSTM_ERR_INVALID_ARG;
+    memset(d, 0, sizeof(*d));
+    int Nx = p->inc_iline == 0 ? 1 : (int)ceil((p->end_iline - p->start_iline) / p->inc_iline);
+    int Ny = p->inc_xline == 0 ? 1 : (int)ceil((p->end_xline - p->start_xline) / p->inc_xline);
+    if (Nx == 0) Nx = 1;
+    if (Ny == 0) Ny = 1;
+    int nx = (int)ceil(1.0 * Nx / p->jobs_x);
+    int ny = (int)ceil(1.0 * Ny / p->jobs_y);
+    if (nx == 0) nx = 1;
+    if (ny == 0) ny = 1;
+    if (Nx < 0 || Ny < 0 || p->job_id < 0 || p->job_id >= p->jobs_x * p->jobs_y)
+        return KPSTM_ERR_INVALID_ARG;
+    d->Nx = Nx;
+    d->Ny = Ny;
+    d->nx = nx;
+    d->ny = ny;
+    d->xslice = p->job_id / p->jobs_y; /* Kirchhoff.c:286-294 */
+    d->yslice = p->job_id % p->jobs_y;
+    d->sinA = (float)sin(p->angle_e_to_n_deg * KO_PI / 180.0); /* :312-313 */
+    d->cosA = (float)cos(p->angle_e_to_n_deg * KO_PI / 180.0);
+    d->ns = p->ns;
+    d->nh = p->output == KPSTM_OUT_STACK ? 1 : p->nh;
+    d->dt = p->dt;
+    d->fs = (float)(2.0 / ((double)p->dt * (double)p->ns)); /* :403 (a/b)/c -> a/(b*c) */
+    return KPSTM_OK;
+}
+
+/* create_aliasfilter, Kirchhoff.c:380-441. */
+int ko_aliasfilter(int ns, float dt, double il_dist, double xl_dist, double cutoff,
+                   int *trange_max, float *anti_alias)
+{
+    if (ns <= 0 || !(dt > 0)) return KPSTM_ERR_INVALID_ARG;
+    float DIP = 45.0f, V_max = 1500.0f;
+    float tanA = (float)tan(DIP * KO_PI / 180.0);
+    float mm = (float)(il_dist <= xl_dist ? il_dist : xl_dist);
+    float fmax = (float)((double)V_max / ((4.0 * (double)mm) * (double)tanA));
+    if (trange_max) *trange_max = (int)floor(0.5 / ((double)fmax * (double)dt));
+    if (!anti_alias) return KPSTM_OK;
+    float fs = (float)(2.0 / ((double)dt * (double)ns));
+    float fm = (float)cutoff;
+    fm = (float)((double)fm * 3.0);
+    float den = ((fm * fm) * fm) * fm;
+    for (int i = 0; i < ns; ++i) anti_alias[i] = 0.0f; /* calloc, Kirchhoff.c:1053 */
+    for (int i = 0; i <= ns / 2; ++i) {
+        float x = (float)i * fs;
+        float num = ((x * x) * x) * x;
+        anti_alias[i] = (float)(1.0 / sqrt(1.0 + (double)(num / den)));
+    }
+    for (int i = ns / 2; i < ns; ++i) anti_alias[i] = anti_alias[ns - i]; /* :419-423 */
+    return KPSTM_OK;
+}
+
+/* Kirchhoff.c:1312-1328. */
+void ko_prep_trace(int ns, int tm, float dt, const float *t2, const float *f, float *P)
+{
+    P[tm] = f[0];
+    for (int t = 1; t < ns; ++t)
+        P[t + tm] = (float)((double)P[t - 1 + tm] + (double)f[t] / (4.0 * (double)t2[t]));
+    for (int t = ns; t < ns + tm; ++t)
+        P[t + tm] = P[t - 1 + tm] + f[ns - 1] / (((dt * dt) * (float)t) * (float)t);
+    for (int t = 1; t < ns + tm; ++t) P[t + tm] = P[t - 1 + tm] + P[t + tm];
+    for (int t = 0; t < tm; ++t) P[t] = P[2 * tm - t];
+}
+
+typedef struct {
+    float sxt, syt, gxt, gyt, cmpx, cmpy;
+    int off, live;
+} ko_geom;
+
+typedef struct {
+    const kpstm_params *p;
+    const kpstm_velocity *v;
+    const ko_dims *d;
+    const float *vel2;     /* [n_iline][n_xline][nsm] v^2 */
+    const float *t2;
+    const int *t1;         /* [ns] velocity time index */
+    const ko_geom *geom;
+    const float *D;        /* [ntr][ns] triangle taps per output index T */
+    int64_t ntr;
+    float *km, *fold;
+    int next_col;
+    pthread_mutex_t mu;
+    int64_t pairs;
+    int err;
+} ko_job;
+
+/* Image loop of Kirchhoff.c:1341-1403 for the columns a worker claims. */
+static void *column_worker(void *arg)
+{
+    ko_job *J = (ko_job *)arg;
+    const kpstm_params *p = J->p;
+    const ko_dims *d = J->d;
+    const int ns = d->ns, nh = d->nh;
+    int64_t pairs = 0;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int col = J->next_col++;
+        pthread_mutex_unlock(&J->mu);
+        if (col >= d->nx * d->ny) break;
+        int xc = col / d->ny, yc = col % d->ny;
+        float IX = (float)((p->start_iline + ((xc + d->xslice * d->nx) * p->inc_iline)) * p->iline_distance);
+        float IY = (float)((p->start_xline + ((yc + d->yslice * d->ny) * p->inc_xline)) * p->xline_distance);
+        int xc1 = (int)round((p->start_iline - J->v->o_iline) / J->v->d_iline +
+                             (xc + d->xslice * d->nx) * (p->inc_iline / J->v->d_iline));
+        int yc1 = (int)round((p->start_xline - J->v->o_xline) / J->v->d_xline +
+                             (yc + d->yslice * d->ny) * (p->inc_xline / J->v->d_xline));
+        if (xc1 > J->v->n_iline - 1) xc1 = J->v->n_iline - 1;
+        if (yc1 > J->v->n_xline - 1) yc1 = J->v->n_xline - 1;
+        const float *v2 = J->vel2 + ((size_t)xc1 * J->v->n_xline + yc1) * J->v->nsm;
+        int bad_vel = (xc1 < 0 || yc1 < 0);
+        float *km = J->km + (size_t)col * nh * ns;
+        float *fold = J->fold + (size_t)col * nh * ns;
+        for (int64_t it = 0; it < J->ntr; ++it) {
+            const ko_geom *g = &J->geom[it];
+            if (!g->live) continue;
+            float dIS2 = (IX - g->sxt) * (IX - g->sxt) + (IY - g->syt) * (IY - g->syt);
+            float dIR2 = (IX - g->gxt) * (IX - g->gxt) + (IY - g->gyt) * (IY - g->gyt);
+            float dIC = sqrtf((IX - g->cmpx) * (IX - g->cmpx) + (IY - g->cmpy) * (IY - g->cmpy));
+            if (!((double)dIC < p->aperture)) continue;
+            if (bad_vel) {
+                pthread_mutex_lock(&J->mu);
+                J->err = KPSTM_ERR_VELOCITY_RANGE;
+                pthread_mutex_unlock(&J->mu);
+                break;
+            }
+            const float *Dt = J->D + (size_t)it * ns;
+            float *k = km + (size_t)g->off * ns;
+            float *f = fold + (size_t)g->off * ns;
+            for (int t = 0; t < ns; ++t) {
+                float vv = v2[J->t1[t]];
+                float s1 = J->t2[t] + dIS2 / vv;
+                float s2 = J->t2[t] + dIR2 / vv;
+                float dsr = (float)(sqrt((double)s1) + sqrt((double)s2));
+                int T = (int)floor(dsr / d->dt);
+                if (T < ns) {
+                    k[t] = k[t] + Dt[T];
+                    f[t] = f[t] + 1.0f;
+                }
+            }
+            pairs += ns;
+        }
+    }
+    pthread_mutex_lock(&J->mu);
+    J->pairs += pairs;
+    pthread_mutex_unlock(&J->mu);
+    return NULL;
+}
+
+int ko_finish(const kpstm_params *p, const float *km, const float *fold, float *image)
+{
+    ko_dims d;
+    int st = ko_dims_of(p, &d);
+    if (st) return st;
+    int ns = d.ns;
+    float *aa = (float *)malloc(sizeof(float) * ns);
+    double *x = (double *)malloc(sizeof(double) * 2 * ns);
+    double *X = (double *)malloc(sizeof(double) * 2 * ns);
+    double *y = (double *)malloc(sizeof(double) * 2 * ns);
+    if (!aa || !x || !X || !y) {
+        free(aa); free(x); free(X); free(y);
+        return KPSTM_ERR_OUT_OF_MEMORY;
+    }
+    ko_aliasfilter(ns, p->dt, p->iline_distance, p->xline_distance, p->anti_alias_cutoff, NULL, aa);
+    float dt = p->dt;
+    size_t ntrace = (size_t)d.nx * d.ny * d.nh;
+    for (size_t tr = 0; tr < ntrace; ++tr) {
+        const float *k = km + tr * ns;
+        const float *f = fold + tr * ns;
+        x[0] = 0.0;
+        x[1] = 0.0;
+        for (int t = 1; t < ns; ++t) { /* Kirchhoff.c:1457-1462 */
+            float v = ((((-dt) * (float)t) * (k[t] - k[t - 1])) * dt) / f[t];
+            x[2 * t] = v;
+            x[2 * t + 1] = 0.0;
+        }
+        kref_dft(ns, FFTW_FORWARD, x, X); /* :1465 */
+        for (int t = 0; t < ns; ++t) {    /* :1467-1473; a,b,c,d are float (:1419) */
+            float a = aa[t], b = 0.0f, c = (float)X[2 * t], e = (float)X[2 * t + 1];
+            X[2 * t] = (double)(a * c - b * e);
+            X[2 * t + 1] = (double)(a * e + b * c);
+        }
+        kref_dft(ns, FFTW_BACKWARD, X, y); /* :1474 */
+        float *o = image + tr * ns;
+        o[0] = 0.0f;
+        for (int t = 1; t < ns; ++t) o[t] = (float)(y[2 * t] / ns); /* :1475-1479 */
+    }
+    free(aa); free(x); free(X); free(y);
+    return KPSTM_OK;
+}
+
+int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be,
+                 const float *samples, int64_t ntr, float *km_out, float *fold_out, float *image,
+                 int nthreads, int64_t *pairs_out)
+{
+    if (!p || !v || !v->vrms || (ntr > 0 && (!hdr_be || !samples)) || ntr < 0)
+        return KPSTM_ERR_INVALID_ARG;
+    if (p->mode != KPSTM_MODE_REFERENCE) return KPSTM_ERR_UNSUPPORTED;
+    ko_dims d;
+    int st = ko_dims_of(p, &d);
+    if (st) return st;
+    const int ns = d.ns, nh = d.nh;
+    int tm;
+    ko_aliasfilter(ns, p->dt, p->iline_distance, p->xline_distance, p->anti_alias_cutoff, &tm, NULL);
+    if (tm < 2) return KPSTM_ERR_TRANGE;
+    d.trange_max = tm;
+
+    size_t nvel = (size_t)v->n_iline * v->n_xline * v->nsm;
+    size_t nimg = (size_t)d.nx * d.ny * nh * ns;
+    float *vel2 = (float *)malloc(sizeof(float) * nvel);
+    float *t2 = (float *)malloc(sizeof(float) * ns);
+    int *t1 = (int *)malloc(sizeof(int) * ns);
+    ko_geom *geom = (ko_geom *)calloc((size_t)(ntr > 0 ? ntr : 1), sizeof(ko_geom));
+    float *D = (float *)malloc(sizeof(float) * (size_t)(ntr > 0 ? ntr : 1) * ns);
+    float *P = (float *)malloc(sizeof(float) * (ns + 2 * tm));
+    float *km = (float *)calloc(nimg, sizeof(float));
+    float *fold = (float *)malloc(sizeof(float) * nimg);
+    if (!vel2 || !t2 || !t1 || !geom || !D || !P || !km || !fold) {
+        st = KPSTM_ERR_OUT_OF_MEMORY;
+        goto done;
+    }
+    for (size_t i = 0; i < nvel; ++i) { /* Kirchhoff.c:612-618 */
+        if (v->vrms[i] == 0.0f) { st = KPSTM_ERR_VELOCITY_ZERO; goto done; }
+        vel2[i] = v->vrms[i] * v->vrms[i];
+    }
+    for (size_t i = 0; i < nimg; ++i) fold[i] = 1.0f; /* :1270 */
+    for (int t = 0; t < ns; ++t) { /* :1246-1247, 1376-1378 */
+        t2[t] = (float)(0.25 * t * t * (double)p->dt * (double)p->dt);
+        int q = (int)round((double)((float)t * (p->dt / v->dtm)));
+        t1[t] = q > v->nsm - 1 ? v->nsm - 1 : q;
+    }
+    /* slab centre and half-diagonal, Kirchhoff.c:1332-1335 */
+    float IXc = (float)((p->start_iline + ((d.nx / 2.0 + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance);
+    float IYc = (float)((p->start_xline + ((d.ny / 2.0 + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance);
+    float add_on = (float)(0.5 * sqrt(d.nx * p->inc_iline * p->iline_distance * d.nx * p->inc_iline * p->iline_distance +
+                                      d.ny * p->inc_xline * p->xline_distance * d.ny * p->inc_xline * p->xline_distance));
+    for (int64_t it = 0; it < ntr; ++it) {
+        const int32_t *h = hdr_be + (size_t)it * 60;
+        double w[4];
+        for (int k = 0; k < 4; ++k) w[k] = (double)be32(h[18 + k]) - (k % 2 == 0 ? p->ox : p->oy);
+        for (int k = 0; k < 4; ++k)
+            if (!(w[k] > -2147483649.0 && w[k] < 2147483648.0)) { st = KPSTM_ERR_GEOMETRY; goto done; }
+        int i = (int)w[0], j = (int)w[1];
+        ko_geom *g = &geom[it];
+        g->sxt = d.cosA * (float)i + d.sinA * (float)j; /* :1297-1299 */
+        g->syt = -d.sinA * (float)i + d.cosA * (float)j;
+        i = (int)w[2];
+        j = (int)w[3];
+        g->gxt = d.cosA * (float)i + d.sinA * (float)j; /* :1302-1304 */
+        g->gyt = -d.sinA * (float)i + d.cosA * (float)j;
+        float h2 = (float)(0.25 * (double)((g->sxt - g->gxt) * (g->sxt - g->gxt) +
+                                           (g->syt - g->gyt) * (g->syt - g->gyt)));
+        g->cmpx = (float)(0.5 * (double)(g->sxt + g->gxt));
+        g->cmpy = (float)(0.5 * (double)(g->syt + g->gyt));
+        int off = (int)floor((2.0 * sqrt((double)h2) - p->oh) / p->dh); /* :1310 */
+        if (p->output == KPSTM_OUT_STACK) off = (off >= 0 && off < p->nh) ? 0 : -1;
+        g->off = off;
+        float dIC = sqrtf((IXc - g->cmpx) * (IXc - g->cmpx) + (IYc - g->cmpy) * (IYc - g->cmpy));
+        g->live = (off >= 0 && off < nh) && ((double)dIC < p->aperture + (double)add_on);
+        if (g->live) {
+            ko_prep_trace(ns, tm, p->dt, t2, samples + (size_t)it * ns, P);
+            float *Dt = D + (size_t)it * ns;
+            for (int T = 0; T < ns; ++T) /* :1391-1392, taps at T and T +- 2 */
+                Dt[T] = (float)(-2.0 * (double)P[T + tm] + (double)P[T + tm - 2] + (double)P[T + tm + 2]);
+        }
+    }
+    {
+        ko_job J;
+        memset(&J, 0, sizeof(J));
+        J.p = p; J.v = v; J.d = &d; J.vel2 = vel2; J.t2 = t2; J.t1 = t1; J.geom = geom; J.D = D;
+        J.ntr = ntr; J.km = km; J.fold = fold;
+        pthread_mutex_init(&J.mu, NULL);
+        if (nthreads <= 0) nthreads = (int)sysconf(_SC_NPROCESSORS_ONLN);
+        if (nthreads < 1) nthreads = 1;
+        if (nthreads > 256) nthreads = 256;
+        pthread_t th[256];
+        int started = 0;
+        for (int k = 0; k < nthreads; ++k)
+            if (pthread_create(&th[k], NULL, column_worker, &J) == 0) started++;
+        if (started == 0) column_worker(&J);
+        for (int k = 0; k < started; ++k) pthread_join(th[k], NULL);
+        pthread_mutex_destroy(&J.mu);
+        if (J.err) { st = J.err; goto done; }
+        if (pairs_out) *pairs_out = J.pairs;
+    }
+    if (km_out) memcpy(km_out, km, sizeof(float) * nimg);
+    if (fold_out) memcpy(fold_out, fold, sizeof(float) * nimg);
+    if (image) st = ko_finish(p, km, fold, image);
+done:
+    free(vel2); free(t2); free(t1); free(geom); free(D); free(P); free(km); free(fold);
+    return st;
+}

@@ -1,0 +1,271 @@
+"""Seeded synthetic surveys for the migration workloads.
+
+The reference ships no data (its Ghana field files are absent), so every
+workload is synthesised from a written description: geometry, sampling,
+events (Ricker wavelets on double-square-root or mirror-source traveltimes),
+v_rms model and noise.  Each survey carries the kpstm_params values and the
+matching compile-time configuration of the reference (Kirchhoff.c:17-65),
+so that the reference, the oracle and the GPU library image the same thing.
+
+Coordinates are integers in the headers because the reference truncates
+header coordinates to int (Kirchhoff.c:1297, 1302).  The 2-D line survey
+(12.5 m CMP spacing) is therefore written in half-metre units: every length,
+the aperture and the velocities are doubled, which leaves all traveltimes
+(and, since the reference's triangle half-width is fixed at 2 samples,
+every imaged value) unchanged.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import segy
+
+
+@dataclass
+class Velocity:
+    n_iline: int
+    n_xline: int
+    nsm: int
+    o_iline: int
+    o_xline: int
+    d_iline: int
+    d_xline: int
+    dtm: float
+    vrms: np.ndarray  # [n_iline, n_xline, nsm] float32
+
+    @property
+    def dtm_us(self) -> int:
+        return int(round(self.dtm * 1e6))
+
+
+@dataclass
+class Survey:
+    name: str
+    params: dict
+    velocity: Velocity
+    headers: np.ndarray          # [ntr, 60] int32, host order
+    samples: np.ndarray          # [ntr, ns] float32 (IBM-representable)
+    info: dict = field(default_factory=dict)
+
+    @property
+    def ntr(self) -> int:
+        return self.headers.shape[0]
+
+    @property
+    def ns(self) -> int:
+        return int(self.params["ns"])
+
+    @property
+    def dt_us(self) -> int:
+        return int(round(self.params["dt"] * 1e6))
+
+    def ref_config(self, jobs_x: int = 1, jobs_y: int = 1, ntblock: int | None = None) -> dict:
+        """Values for the reference's #define block (Kirchhoff.c:17-65)."""
+        p, v = self.params, self.velocity
+        return dict(
+            NVel_ilines=v.n_iline, NVel_xlines=v.n_xline, dVel_ilines=v.d_iline,
+            dVel_xlines=v.d_xline, oVel_ilines=v.o_iline, oVel_xlines=v.o_xline,
+            Startiline=p["start_iline"], Endiline=p["end_iline"],
+            Startxline=p["start_xline"], Endxline=p["end_xline"],
+            INCiline=p["inc_iline"], INCxline=p["inc_xline"], dh=p["dh"], nh=p["nh"],
+            oh=p["oh"], ox=p["ox"], oy=p["oy"], angleEtoN=p["angle_e_to_n_deg"],
+            iline_distance=p["iline_distance"], xline_distance=p["xline_distance"],
+            aperture=p["aperture"], anti_alias_cutoff=p["anti_alias_cutoff"],
+            ntblock=ntblock or max(1, self.ntr), number_mpi_jobsX=jobs_x,
+            number_mpi_jobsY=jobs_y)
+
+    def write_files(self, data_path, vel_path) -> None:
+        segy.write_segy(data_path, self.headers, self.samples)
+        v = self.velocity
+        vh = segy.velocity_headers(v.n_iline, v.n_xline, v.o_iline, v.o_xline,
+                                   v.d_iline, v.d_xline, v.nsm, v.dtm_us)
+        segy.write_segy(vel_path, vh, v.vrms.reshape(v.n_iline * v.n_xline, v.nsm))
+
+
+def default_params(**kw) -> dict:
+    p = dict(ns=0, dt=0.0, start_iline=0, end_iline=0, start_xline=0, end_xline=0,
+             inc_iline=1.0, inc_xline=1.0, iline_distance=25.0, xline_distance=25.0,
+             nh=1, oh=0.0, dh=1.0, ox=0.0, oy=0.0, angle_e_to_n_deg=0.0, xy_scale=1.0,
+             aperture=3000.0, anti_alias_cutoff=50.0, jobs_x=1, jobs_y=1, job_id=0,
+             mode=0, precision=0, output=0, aa_max_halfwidth=0)
+    p.update(kw)
+    return p
+
+
+def ricker(tau: np.ndarray, f: float) -> np.ndarray:
+    a = (math.pi * f * tau) ** 2
+    return (1.0 - 2.0 * a) * np.exp(-a)
+
+
+def _add_events(samples: np.ndarray, t_event: np.ndarray, amp: np.ndarray, dt: float,
+                f: float, half_width: int) -> None:
+    """samples[i, :] += amp[i, e] * ricker(t - t_event[i, e]) over a window."""
+    ntr, ns = samples.shape
+    k = np.arange(-half_width, half_width + 1)
+    for e in range(t_event.shape[1]):
+        te = t_event[:, e]
+        c = np.floor(te / dt).astype(np.int64)
+        idx = c[:, None] + k[None, :]
+        ok = (idx >= 0) & (idx < ns)
+        w = ricker(idx * dt - te[:, None], f) * amp[:, e:e + 1]
+        rows = np.broadcast_to(np.arange(ntr)[:, None], idx.shape)
+        np.add.at(samples, (rows[ok], idx[ok]), w[ok])
+
+
+def line2d(n_cmp: int = 200, n_off: int = 48, ns: int = 1001, dt: float = 0.004,
+           n_scat: int = 20, snr_db: float = 20.0, seed: int = 1,
+           aperture_m: float = 1500.0, aa_cutoff: float = 1.0e6,
+           name: str = "line2d") -> Survey:
+    """2-D line: n_cmp CMPs at 12.5 m x n_off offsets (0, 50, ... m), point
+    scatterers with 25 Hz Ricker diffraction hyperbolae, v_rms = 1500 +
+    600*t0 m/s, Gaussian noise at ``snr_db``; image n_cmp columns x n_off
+    classes x ns.  Anti-alias "off" is a cutoff far above Nyquist: the
+    reference's [1,2,1] triangle taps are intrinsic to its operator
+    (Kirchhoff.c:1391-1392), only its low-pass can be switched off.
+
+    Half-metre units (see module docstring): CMP spacing 25, offsets 100.
+    """
+    rng = np.random.default_rng(seed)
+    u = 2.0                                     # units per metre
+    d_cmp = 12.5 * u                            # 25 units
+    start_il = 96                               # IX = start_il * 25 = 2400 units
+    x0 = start_il * d_cmp
+    y_line = 4 * d_cmp                          # xline 4
+    cmp_x = x0 + d_cmp * np.arange(n_cmp)
+    half = 25.0 * u * np.arange(n_off)          # half-offsets (units)
+    mx = np.repeat(cmp_x, n_off)
+    hh = np.tile(half, n_cmp)
+    sx = (mx - hh).astype(np.int64)
+    gx = (mx + hh).astype(np.int64)
+    if sx.min() < 0:
+        raise ValueError("survey extends below coordinate 0")
+    sy = np.full_like(sx, int(y_line))
+    gy = sy.copy()
+    ntr = sx.size
+
+    # scatterers
+    px = rng.uniform(cmp_x[0], cmp_x[-1], n_scat)
+    pt0 = rng.uniform(0.4, 3.6, n_scat)
+    pamp = rng.uniform(0.5, 1.0, n_scat)
+    pv = (1500.0 + 600.0 * pt0) * u
+    ts = np.sqrt(0.25 * pt0[None, :] ** 2 + ((sx[:, None] - px[None, :]) / pv[None, :]) ** 2)
+    tg = np.sqrt(0.25 * pt0[None, :] ** 2 + ((gx[:, None] - px[None, :]) / pv[None, :]) ** 2)
+    samples = np.zeros((ntr, ns), dtype=np.float64)
+    _add_events(samples, ts + tg, np.broadcast_to(pamp, (ntr, n_scat)).copy(), dt, 25.0,
+                half_width=int(math.ceil(0.08 / dt)))
+    sig_rms = float(np.sqrt(np.mean(samples ** 2)))
+    if snr_db is not None and sig_rms > 0:
+        samples += rng.normal(0.0, sig_rms / 10.0 ** (snr_db / 20.0), samples.shape)
+    samples = segy.ibm_roundtrip(samples.astype(np.float32))
+    hdr = segy.trace_headers(sx, sy, gx, gy, ns, int(round(dt * 1e6)),
+                             {segy.W_OFFSET: (gx - sx)})
+
+    nsm = ns
+    t0 = np.arange(nsm) * dt
+    vt = ((1500.0 + 600.0 * t0) * u).astype(np.float32)
+    vel = Velocity(n_iline=n_cmp, n_xline=1, nsm=nsm, o_iline=start_il, o_xline=4,
+                   d_iline=1, d_xline=1, dtm=dt,
+                   vrms=segy.ibm_roundtrip(np.broadcast_to(vt, (n_cmp, 1, nsm)).copy()))
+    params = default_params(
+        ns=ns, dt=float(np.float32(int(round(dt * 1e6)) / 1e6)),
+        start_iline=start_il, end_iline=start_il + n_cmp, start_xline=4, end_xline=4,
+        iline_distance=d_cmp, xline_distance=d_cmp, nh=n_off, oh=-50.0 * u / 2.0 * 1.0,
+        dh=50.0 * u, aperture=aperture_m * u, anti_alias_cutoff=aa_cutoff)
+    # oh = -dh/2 centres each class on its nominal offset: class k holds
+    # offsets in [100k - 50, 100k + 50) units, so no offset sits on a class edge.
+    params["oh"] = -0.5 * params["dh"]
+    info = dict(units_per_metre=u, scatterers=np.stack([px, pt0, pamp], 1), seed=seed)
+    return Survey(name, params, vel, hdr, samples, info)
+
+
+def vrms_3d(x: np.ndarray, t0: np.ndarray, v0: float, vt: float, va: float,
+            lam: float) -> np.ndarray:
+    """v_rms(x, t0) = v0 + vt*t0 + va*sin(2*pi*x/lam)."""
+    return v0 + vt * t0 + va * np.sin(2.0 * math.pi * x / lam)
+
+
+def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int = 400,
+            bin_m: float = 25.0, max_offset: float = 4000.0, n_refl: int = 8,
+            n_diff: int = 200, freq: float = 30.0, aperture: float = 3000.0,
+            aa_cutoff: float = 100.0, seed: int = 2, mode: int = 1, output: int = 1,
+            nh: int = 1, oh: float = 0.0, dh: float = 1.0e9, offsets=None,
+            v_law=(1600.0, 500.0, 100.0, 8000.0), name: str = "patch3d",
+            trace_slice: slice | None = None) -> Survey:
+    """3-D patch: midpoints uniform over nx*bin x ny*bin metres, offsets
+    U(0, max_offset) (or the given array), azimuths U(0, 2 pi); 30 Hz Ricker
+    events from ``n_refl`` planar dipping reflectors (dips U(0, 30 deg),
+    mirror-source traveltimes in a constant velocity per reflector) plus
+    ``n_diff`` point diffractors (DSR traveltimes); smooth v_rms(x, t0) =
+    v0 + vt*t0 + va*sin(2 pi x / lam).  Image nx x ny x ns at ``bin_m``.
+    ``trace_slice`` keeps only those traces (same seeded survey)."""
+    rng = np.random.default_rng(seed)
+    start = int(math.ceil(max_offset / 2.0 / bin_m)) + 4
+    x0 = start * bin_m
+    y0 = start * bin_m
+    W, H = nx * bin_m, ny * bin_m
+    mxs = rng.uniform(x0, x0 + W, ntr)
+    mys = rng.uniform(y0, y0 + H, ntr)
+    off = rng.uniform(0.0, max_offset, ntr) if offsets is None else np.asarray(offsets, float)
+    az = rng.uniform(0.0, 2.0 * math.pi, ntr)
+    v0, vt, va, lam = v_law
+    # events (drawn before slicing so every slice sees the same model)
+    r_t0 = rng.uniform(0.4, 0.8 * (ns - 1) * dt, n_refl)
+    r_dip = np.radians(rng.uniform(0.0, 30.0, n_refl))
+    r_az = rng.uniform(0.0, 2.0 * math.pi, n_refl)
+    r_amp = rng.uniform(0.5, 1.0, n_refl) * rng.choice([-1.0, 1.0], n_refl)
+    d_x = rng.uniform(x0, x0 + W, n_diff)
+    d_y = rng.uniform(y0, y0 + H, n_diff)
+    d_t0 = rng.uniform(0.4, 0.9 * (ns - 1) * dt, n_diff)
+    d_amp = rng.uniform(0.5, 1.0, n_diff)
+    if trace_slice is not None:
+        mxs, mys, off, az = mxs[trace_slice], mys[trace_slice], off[trace_slice], az[trace_slice]
+    h = 0.5 * off
+    sx = np.rint(mxs - h * np.cos(az)).astype(np.int64)
+    sy = np.rint(mys - h * np.sin(az)).astype(np.int64)
+    gx = np.rint(mxs + h * np.cos(az)).astype(np.int64)
+    gy = np.rint(mys + h * np.sin(az)).astype(np.int64)
+    if min(sx.min(), sy.min(), gx.min(), gy.min()) < 0:
+        raise ValueError("survey extends below coordinate 0")
+    n = sx.size
+    samples = np.zeros((n, ns), dtype=np.float64)
+    hw = int(math.ceil(0.06 / dt))
+    xc, yc = x0 + 0.5 * W, y0 + 0.5 * H
+    # planar reflectors: plane through (xc, yc, z0) with unit normal nrm
+    for k in range(n_refl):
+        vk = v0 + vt * r_t0[k]
+        z0 = 0.5 * vk * r_t0[k]
+        nrm = np.array([math.sin(r_dip[k]) * math.cos(r_az[k]),
+                        math.sin(r_dip[k]) * math.sin(r_az[k]), math.cos(r_dip[k])])
+        dist_s = nrm[2] * z0 - (nrm[0] * (sx - xc) + nrm[1] * (sy - yc))
+        mx_ = sx + 2.0 * dist_s * nrm[0]
+        my_ = sy + 2.0 * dist_s * nrm[1]
+        mz_ = 2.0 * dist_s * nrm[2]
+        te = np.sqrt((mx_ - gx) ** 2 + (my_ - gy) ** 2 + mz_ ** 2) / vk
+        _add_events(samples, te[:, None], np.full((n, 1), r_amp[k]), dt, freq, hw)
+    # diffractors (chunks bound memory)
+    dv = vrms_3d(d_x, d_t0, v0, vt, va, lam)
+    for c0 in range(0, n_diff, 32):
+        c1 = min(n_diff, c0 + 32)
+        ts = np.sqrt(0.25 * d_t0[None, c0:c1] ** 2 + ((sx[:, None] - d_x[None, c0:c1]) ** 2 +
+                                                      (sy[:, None] - d_y[None, c0:c1]) ** 2) / dv[None, c0:c1] ** 2)
+        tg = np.sqrt(0.25 * d_t0[None, c0:c1] ** 2 + ((gx[:, None] - d_x[None, c0:c1]) ** 2 +
+                                                      (gy[:, None] - d_y[None, c0:c1]) ** 2) / dv[None, c0:c1] ** 2)
+        _add_events(samples, ts + tg, np.broadcast_to(d_amp[c0:c1], (n, c1 - c0)).copy(), dt, freq, hw)
+    samples = segy.ibm_roundtrip(samples.astype(np.float32))
+    hdr = segy.trace_headers(sx, sy, gx, gy, ns, int(round(dt * 1e6)))
+    # velocity grid at the image inlines (v does not depend on y)
+    t0 = np.arange(ns) * dt
+    xs = (start + np.arange(nx)) * bin_m
+    vg = vrms_3d(xs[:, None], t0[None, :], v0, vt, va, lam).astype(np.float32)
+    vel = Velocity(n_iline=nx, n_xline=1, nsm=ns, o_iline=start, o_xline=start, d_iline=1,
+                   d_xline=1000000, dtm=dt, vrms=segy.ibm_roundtrip(vg[:, None, :].copy()))
+    params = default_params(
+        ns=ns, dt=float(np.float32(int(round(dt * 1e6)) / 1e6)), start_iline=start,
+        end_iline=start + nx, start_xline=start, end_xline=start + ny,
+        iline_distance=bin_m, xline_distance=bin_m, nh=nh, oh=oh, dh=dh, aperture=aperture,
+        anti_alias_cutoff=aa_cutoff, mode=mode, output=output)
+    info = dict(seed=seed, x0=x0, y0=y0)
+    return Survey(name, params, vel, hdr, samples, info)
