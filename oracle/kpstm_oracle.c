@@ -106,6 +106,8 @@ typedef struct {
     const int *t1;         /* [ns] velocity time index */
     const ko_geom *geom;
     const float *D;        /* [ntr][ns] triangle taps per output index T */
+    const float *P;        /* full mode: [ntr][ns + 2*tm] double running integral */
+    int tm, lmax;
     int64_t ntr;
     float *km, *fold;
     int next_col;
@@ -113,6 +115,54 @@ typedef struct {
     int64_t pairs;
     int err;
 } ko_job;
+
+/* Linear interpolation of the running integral at fractional index x
+   (sample units; P[tm + i] holds index i). */
+static double interp(const float *P, int tm, double x)
+{
+    double fl = floor(x);
+    int i = (int)fl + tm;
+    double fr = x - fl;
+    return (double)P[i] + fr * ((double)P[i + 1] - (double)P[i]);
+}
+
+/* Full-physics operator (no counterpart in the reference; the GPU's
+   KPSTM_MODE_FULL), in double: tau = ts + tr with
+   ts = sqrt((t0/2)^2 + |I-S|^2/v^2); a triangle of real half-width
+   Lf = clamp(1 + |dtau/dx| dx/dt + |dtau/dy| dy/dt, 1, lmax) read from the
+   double running integral as [P(T-1+Lf) - 2P(T-1) + P(T-1-Lf)]/Lf^2 at
+   T = tau/dt (linear interpolation); weight t0 (1/ts + 1/tr)^2 / 8. */
+static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, const float *v2,
+                       const float *P, float *k, float *f)
+{
+    const kpstm_params *p = J->p;
+    const int ns = J->d->ns, tm = J->tm;
+    const double dt = (double)J->d->dt;
+    const double sx = (double)IX - g->sxt, sy = (double)IY - g->syt;
+    const double gx = (double)IX - g->gxt, gy = (double)IY - g->gyt;
+    const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
+    const double ax = p->iline_distance / dt, ay = p->xline_distance / dt;
+    for (int t = 0; t < ns; ++t) {
+        double rv2 = 1.0 / (double)v2[J->t1[t]];
+        double t0 = (double)t * dt;
+        double th2 = 0.25 * t0 * t0;
+        double as = th2 + dS2 * rv2, ar = th2 + dR2 * rv2;
+        if (as < 1e-30) as = 1e-30;
+        if (ar < 1e-30) ar = 1e-30;
+        double ts = sqrt(as), tr = sqrt(ar);
+        double Tf = (ts + tr) / dt;
+        if (!(Tf < ns - 1)) continue;
+        double slx = (sx / ts + gx / tr) * rv2 * ax, sly = (sy / ts + gy / tr) * rv2 * ay;
+        double Lf = 1.0 + fabs(slx) + fabs(sly);
+        if (Lf > J->lmax) Lf = J->lmax;
+        double x0 = Tf - 1.0;
+        double tri = (interp(P, tm, x0 + Lf) - 2.0 * interp(P, tm, x0) + interp(P, tm, x0 - Lf)) / (Lf * Lf);
+        double u = 1.0 / ts + 1.0 / tr;
+        double w = t0 / 8.0 * u * u;
+        k[t] = (float)((double)k[t] + w * tri);
+        f[t] = f[t] + 1.0f;
+    }
+}
 
 /* Image loop of Kirchhoff.c:1341-1403 for the columns a worker claims. */
 static void *column_worker(void *arg)
@@ -153,9 +203,14 @@ static void *column_worker(void *arg)
                 pthread_mutex_unlock(&J->mu);
                 break;
             }
-            const float *Dt = J->D + (size_t)it * ns;
             float *k = km + (size_t)g->off * ns;
             float *f = fold + (size_t)g->off * ns;
+            if (p->mode == KPSTM_MODE_FULL) {
+                full_pairs(J, g, IX, IY, v2, J->P + (size_t)it * (ns + 2 * J->tm), k, f);
+                pairs += ns;
+                continue;
+            }
+            const float *Dt = J->D + (size_t)it * ns;
             for (int t = 0; t < ns; ++t) {
                 float vv = v2[J->t1[t]];
                 float s1 = J->t2[t] + dIS2 / vv;
@@ -224,7 +279,8 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
 {
     if (!p || !v || !v->vrms || (ntr > 0 && (!hdr_be || !samples)) || ntr < 0)
         return KPSTM_ERR_INVALID_ARG;
-    if (p->mode != KPSTM_MODE_REFERENCE) return KPSTM_ERR_UNSUPPORTED;
+    if (p->mode != KPSTM_MODE_REFERENCE && p->mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED;
+    const int full = p->mode == KPSTM_MODE_FULL;
     ko_dims d;
     int st = ko_dims_of(p, &d);
     if (st) return st;
@@ -240,8 +296,9 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
     float *t2 = (float *)malloc(sizeof(float) * ns);
     int *t1 = (int *)malloc(sizeof(int) * ns);
     ko_geom *geom = (ko_geom *)calloc((size_t)(ntr > 0 ? ntr : 1), sizeof(ko_geom));
-    float *D = (float *)malloc(sizeof(float) * (size_t)(ntr > 0 ? ntr : 1) * ns);
-    float *P = (float *)malloc(sizeof(float) * (ns + 2 * tm));
+    const size_t prow = (size_t)ns + 2 * tm;
+    float *D = (float *)malloc(sizeof(float) * (size_t)(ntr > 0 ? ntr : 1) * (full ? prow : (size_t)ns));
+    float *P = (float *)malloc(sizeof(float) * prow);
     float *km = (float *)calloc(nimg, sizeof(float));
     float *fold = (float *)malloc(sizeof(float) * nimg);
     if (!vel2 || !t2 || !t1 || !geom || !D || !P || !km || !fold) {
@@ -286,7 +343,9 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
         g->off = off;
         float dIC = sqrtf((IXc - g->cmpx) * (IXc - g->cmpx) + (IYc - g->cmpy) * (IYc - g->cmpy));
         g->live = (off >= 0 && off < nh) && ((double)dIC < p->aperture + (double)add_on);
-        if (g->live) {
+        if (g->live && full) {
+            ko_prep_trace(ns, tm, p->dt, t2, samples + (size_t)it * ns, D + (size_t)it * prow);
+        } else if (g->live) {
             ko_prep_trace(ns, tm, p->dt, t2, samples + (size_t)it * ns, P);
             float *Dt = D + (size_t)it * ns;
             for (int T = 0; T < ns; ++T) /* :1391-1392, taps at T and T +- 2 */
@@ -297,6 +356,15 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
         ko_job J;
         memset(&J, 0, sizeof(J));
         J.p = p; J.v = v; J.d = &d; J.vel2 = vel2; J.t2 = t2; J.t1 = t1; J.geom = geom; J.D = D;
+        J.P = D;
+        J.tm = tm;
+        {
+            int lmax = p->aa_max_halfwidth > 0 ? p->aa_max_halfwidth : tm - 1;
+            if (lmax > tm - 1) lmax = tm - 1;
+            if (lmax > 63) lmax = 63;
+            if (lmax < 1) lmax = 1;
+            J.lmax = lmax;
+        }
         J.ntr = ntr; J.km = km; J.fold = fold;
         pthread_mutex_init(&J.mu, NULL);
         if (nthreads <= 0) nthreads = (int)sysconf(_SC_NPROCESSORS_ONLN);

@@ -1,0 +1,661 @@
+/*
+ * libkpstm: context, device memory, streams and the C ABI of include/kpstm.h.
+ *
+ * One context images one slab (job) of the reference's image box.  It owns
+ * a compute stream and a copy stream: kpstm_add_traces copies block b+1 to
+ * the device (copy stream) while block b is imaged (compute stream), using
+ * two staging slots; the call returns once its own host buffers have been
+ * read.  Per block the compute stream runs
+ *     k_geometry -> k_bucket -> k_prep -> k_image
+ * with no host synchronisation; kpstm_finish runs k_deriv -> k_lowpass.
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "kpstm_kernels.cuh"
+
+#define KP_CUDA(call)                                                                                        \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess) {                                                                             \
+            return e_ == cudaErrorMemoryAllocation ? KPSTM_ERR_OUT_OF_MEMORY : KPSTM_ERR_CUDA;               \
+        }                                                                                                    \
+    } while (0)
+
+struct kpstm_ctx {
+    kpstm_params p;
+    kpstm_setup s;
+    int device;
+    int finished_state; /* reserved */
+    cudaStream_t cs, xs;         /* compute, copy */
+    cudaEvent_t copy_done[2], comp_done[2];
+    int slot;
+    int K, nwin, ntile;
+    int64_t row;                 /* floats per tap-table row */
+    /* constant tables */
+    float2 *d_colxy;
+    int32_t *d_colrow;
+    float4 *d_tilebox;
+    float2 *d_vrows;
+    float *d_t2;
+    float2 *d_t2c;
+    double *d_c4, *d_c4r;
+    float *d_h;
+    float *d_invl2;
+    /* image */
+    float *d_km, *d_kc;
+    int32_t *d_cnt;
+    /* per-block work buffers (compute stream) */
+    int64_t cap;                 /* traces */
+    kpstm_geom *d_graw, *d_geom;
+    int32_t *d_cls, *d_order, *d_cstart, *d_nlive;
+    float *d_table;
+    /* staging (two slots) */
+    int64_t scap;
+    int32_t *d_hdr[2];
+    float *d_smp[2];
+    uint32_t *d_raw;
+    int64_t rawcap;
+    /* status */
+    int *d_status;
+    unsigned long long *d_hits;
+    /* finishing scratch */
+    float *d_x, *d_y;
+};
+
+static int kp_free_all(kpstm_ctx *c);
+
+static size_t image_smem(const kpstm_ctx *c)
+{
+    const int W = 32 * c->K;
+    const int TB = c->p.mode == KPSTM_MODE_FULL ? KP_TB_FULL : KP_TB_REF;
+    size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * 2 * TB * c->row +
+               sizeof(int32_t) * (KP_LCH + 8 + 2);
+    b = (b + 7) & ~size_t(7);
+    return b + 2 * sizeof(uint64_t);
+}
+
+template <int K>
+static cudaError_t launch_image_k(const kpstm_ctx *c, const KpImageArgs &a, dim3 grid, size_t smem)
+{
+    const bool full = c->p.mode == KPSTM_MODE_FULL;
+    const bool kahan = c->p.precision == KPSTM_PREC_BF16_KAHAN;
+    void (*fn)(KpImageArgs);
+    if (full)
+        fn = kahan ? k_image<K, true, true> : k_image<K, true, false>;
+    else
+        fn = kahan ? k_image<K, false, true> : k_image<K, false, false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, KP_THREADS, smem, c->cs>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_image(const kpstm_ctx *c, const KpImageArgs &a)
+{
+    dim3 grid(c->ntile, c->s.nclass, c->nwin);
+    size_t smem = image_smem(c);
+    switch (c->K) {
+    case 8: return launch_image_k<8>(c, a, grid, smem);
+    case 16: return launch_image_k<16>(c, a, grid, smem);
+    case 24: return launch_image_k<24>(c, a, grid, smem);
+    default: return launch_image_k<32>(c, a, grid, smem);
+    }
+}
+
+static int grow_work(kpstm_ctx *c, int64_t ntr)
+{
+    if (ntr <= c->cap) return KPSTM_OK;
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    cudaFree(c->d_graw);
+    cudaFree(c->d_geom);
+    cudaFree(c->d_cls);
+    cudaFree(c->d_order);
+    cudaFree(c->d_table);
+    c->d_graw = c->d_geom = nullptr;
+    c->d_cls = c->d_order = nullptr;
+    c->d_table = nullptr;
+    c->cap = 0;
+    int64_t n = ntr + ntr / 8 + 64;
+    KP_CUDA(cudaMalloc(&c->d_graw, sizeof(kpstm_geom) * n));
+    KP_CUDA(cudaMalloc(&c->d_geom, sizeof(kpstm_geom) * n));
+    KP_CUDA(cudaMalloc(&c->d_cls, sizeof(int32_t) * n));
+    KP_CUDA(cudaMalloc(&c->d_order, sizeof(int32_t) * n));
+    KP_CUDA(cudaMalloc(&c->d_table, sizeof(float) * c->row * n));
+    c->cap = n;
+    return KPSTM_OK;
+}
+
+static int grow_stage(kpstm_ctx *c, int64_t ntr)
+{
+    if (ntr <= c->scap) return KPSTM_OK;
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    for (int s = 0; s < 2; ++s) {
+        cudaFree(c->d_hdr[s]);
+        cudaFree(c->d_smp[s]);
+        c->d_hdr[s] = nullptr;
+        c->d_smp[s] = nullptr;
+    }
+    c->scap = 0;
+    int64_t n = ntr + ntr / 8 + 64;
+    for (int s = 0; s < 2; ++s) {
+        KP_CUDA(cudaMalloc(&c->d_hdr[s], sizeof(int32_t) * 60 * n));
+        KP_CUDA(cudaMalloc(&c->d_smp[s], sizeof(float) * c->p.ns * n));
+    }
+    c->scap = n;
+    return KPSTM_OK;
+}
+
+/* The per-block device pipeline on the compute stream. */
+static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int64_t ntr)
+{
+    if (ntr == 0) return KPSTM_OK;
+    int st = grow_work(c, ntr);
+    if (st) return st;
+    const kpstm_params *p = &c->p;
+    const kpstm_setup *s = &c->s;
+
+    KpGeomArgs g;
+    g.hdr_be = d_hdr;
+    g.ntr = ntr;
+    g.geom = c->d_graw;
+    g.cls = c->d_cls;
+    g.status = c->d_status;
+    g.ox = p->ox;
+    g.oy = p->oy;
+    g.xy_scale = p->xy_scale;
+    g.oh = p->oh;
+    g.dh = p->dh;
+    g.cull_radius = s->cull_radius;
+    g.sinA = s->sinA;
+    g.cosA = s->cosA;
+    g.IXc = s->IXc;
+    g.IYc = s->IYc;
+    g.nh = p->nh;
+    g.stack = p->output == KPSTM_OUT_STACK;
+    k_geometry<<<(unsigned)((ntr + 255) / 256), 256, 0, c->cs>>>(g);
+    KP_CUDA(cudaGetLastError());
+
+    k_bucket<<<1, 1024, sizeof(int32_t) * (s->nclass + 1), c->cs>>>(c->d_cls, ntr, s->nclass, c->d_cstart,
+                                                                     c->d_order, c->d_nlive);
+    KP_CUDA(cudaGetLastError());
+
+    KpPrepArgs pa;
+    memset(&pa, 0, sizeof(pa));
+    pa.samples = d_smp;
+    pa.geom_raw = c->d_graw;
+    pa.order = c->d_order;
+    pa.nlive = c->d_nlive;
+    pa.geom = c->d_geom;
+    pa.table = c->d_table;
+    pa.c4 = c->d_c4;
+    pa.c4r = c->d_c4r;
+    pa.row = c->row;
+    pa.ns = p->ns;
+    pa.tm = s->dims.trange_max;
+    pa.full = p->mode == KPSTM_MODE_FULL;
+    pa.dt = p->dt;
+    k_prep<<<(unsigned)((ntr + 127) / 128), 128, 0, c->cs>>>(pa);
+    KP_CUDA(cudaGetLastError());
+
+    KpImageArgs a;
+    memset(&a, 0, sizeof(a));
+    a.geom = c->d_geom;
+    a.class_start = c->d_cstart;
+    a.table = c->d_table;
+    a.row = c->row;
+    a.colxy = c->d_colxy;
+    a.colrow = c->d_colrow;
+    a.tilebox = c->d_tilebox;
+    a.vrows = c->d_vrows;
+    a.t2 = c->d_t2;
+    a.t2c = c->d_t2c;
+    a.inv_l2 = c->d_invl2;
+    a.km = c->d_km;
+    a.kc = c->d_kc;
+    a.cnt = c->d_cnt;
+    a.hits = c->d_hits;
+    a.status = c->d_status;
+    a.ncol = s->ncol;
+    a.ns = p->ns;
+    a.tm = s->dims.trange_max;
+    a.lmax = s->lmax;
+    a.lmaxf = (float)s->lmax;
+    a.dt = p->dt;
+    a.rdt = 1.0f / p->dt;
+    a.nsf = (float)p->ns;
+    a.aperture = p->aperture;
+    float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
+    a.tile_r2 = r * r;
+    a.aax = (float)(p->iline_distance / p->dt);
+    a.aay = (float)(p->xline_distance / p->dt);
+    KP_CUDA(launch_image(c, a));
+    return KPSTM_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+
+extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *vel, kpstm_ctx **out)
+{
+    if (!params || !vel || !out) return KPSTM_ERR_INVALID_ARG;
+    *out = nullptr;
+    kpstm_setup s;
+    int st = kpstm_setup_of(params, &s);
+    if (st) return st;
+    st = kpstm_velocity_check(params, vel, &s);
+    if (st) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return KPSTM_ERR_NO_DEVICE;
+
+    kpstm_ctx *c = (kpstm_ctx *)calloc(1, sizeof(kpstm_ctx));
+    if (!c) return KPSTM_ERR_OUT_OF_MEMORY;
+    c->p = *params;
+    c->s = s;
+    cudaGetDevice(&c->device);
+    const int ns = params->ns, tm = s.dims.trange_max;
+    const int ncol = s.ncol;
+    c->nwin = (ns + 1023) / 1024;
+    int per = (ns + c->nwin - 1) / c->nwin;
+    c->K = per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
+    c->ntile = (ncol + KPSTM_COLS_PER_CTA - 1) / KPSTM_COLS_PER_CTA;
+    if (params->mode == KPSTM_MODE_FULL)
+        c->row = ((2 * (int64_t)(ns + 2 * tm - 3)) + 3) & ~int64_t(3);
+    else
+        c->row = (ns + 3) & ~3;
+
+    /* host tables */
+    float *colxy = (float *)malloc(sizeof(float) * 2 * ncol);
+    int32_t *colrow = (int32_t *)malloc(sizeof(int32_t) * ncol);
+    float *t2 = (float *)malloc(sizeof(float) * ns);
+    int32_t *t1 = (int32_t *)malloc(sizeof(int32_t) * ns);
+    double *c4 = (double *)malloc(sizeof(double) * ns);
+    double *c4r = (double *)malloc(sizeof(double) * ns);
+    float2 *t2c = (float2 *)malloc(sizeof(float2) * ns);
+    double *hd = (double *)malloc(sizeof(double) * ns);
+    float *hf = (float *)malloc(sizeof(float) * ns);
+    float4 *box = (float4 *)malloc(sizeof(float4) * c->ntile);
+    int32_t *rowmap = nullptr;
+    float2 *vrows = nullptr;
+    float invl2[64];
+    int nrow = 0;
+    do {
+        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !hd || !hf || !box) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        kpstm_columns(params, vel, &s, colxy, colrow);
+        kpstm_time_tables(params, vel, t2, t1);
+        for (int t = 0; t < ns; ++t) {
+            c4[t] = 4.0 * (double)t2[t];
+            c4r[t] = t > 0 ? 1.0 / c4[t] : 0.0;
+            double t0 = (double)t * (double)params->dt;
+            t2c[t] = make_float2((float)(0.25 * t0 * t0), (float)(t0 / 8.0));
+        }
+        st = kpstm_lowpass_kernel(params, hd);
+        if (st) break;
+        for (int t = 0; t < ns; ++t) hf[t] = (float)hd[t];
+        for (int b = 0; b < c->ntile; ++b) {
+            float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+            for (int k = 0; k < KPSTM_COLS_PER_CTA; ++k) {
+                int cc = b * KPSTM_COLS_PER_CTA + k;
+                if (cc >= ncol) break;
+                x0 = fminf(x0, colxy[2 * cc]);
+                x1 = fmaxf(x1, colxy[2 * cc]);
+                y0 = fminf(y0, colxy[2 * cc + 1]);
+                y1 = fmaxf(y1, colxy[2 * cc + 1]);
+            }
+            box[b] = make_float4(x0, x1, y0, y1);
+        }
+        /* compact the velocity rows the slab uses; v^2 in float as
+           Kirchhoff.c:617, RN(1/v^2) for the exact division */
+        int64_t ngrid = (int64_t)vel->n_iline * vel->n_xline;
+        rowmap = (int32_t *)malloc(sizeof(int32_t) * ngrid);
+        if (!rowmap) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        for (int64_t i = 0; i < ngrid; ++i) rowmap[i] = -1;
+        for (int cc = 0; cc < ncol; ++cc) {
+            int r = colrow[cc];
+            if (r < 0) continue;
+            if (rowmap[r] < 0) rowmap[r] = nrow++;
+            colrow[cc] = rowmap[r];
+        }
+        vrows = (float2 *)malloc(sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns);
+        if (!vrows) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        for (int64_t i = 0; i < ngrid; ++i) {
+            int r = rowmap[i];
+            if (r < 0) continue;
+            const float *v = vel->vrms + i * vel->nsm;
+            for (int t = 0; t < ns; ++t) {
+                float vv = v[t1[t]] * v[t1[t]];
+                vrows[(size_t)r * ns + t] = make_float2(vv, 1.0f / vv);
+            }
+        }
+        for (int L = 0; L < 64; ++L) invl2[L] = L > 0 ? 1.0f / (float)(L * L) : 0.0f;
+    } while (0);
+
+    if (!st) {
+        do {
+            cudaError_t e = cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xs, cudaStreamNonBlocking);
+            for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+                e = cudaEventCreateWithFlags(&c->copy_done[k], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->comp_done[k], cudaEventDisableTiming);
+            }
+            if (e != cudaSuccess) {
+                st = KPSTM_ERR_CUDA;
+                break;
+            }
+            size_t nimg = (size_t)s.nclass * ncol * ns;
+#define KP_ALLOC(ptr, bytes)                                                                                 \
+    if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) {                                                        \
+        st = KPSTM_ERR_OUT_OF_MEMORY;                                                                        \
+        break;                                                                                               \
+    }
+            KP_ALLOC(c->d_colxy, sizeof(float2) * ncol);
+            KP_ALLOC(c->d_colrow, sizeof(int32_t) * ncol);
+            KP_ALLOC(c->d_tilebox, sizeof(float4) * c->ntile);
+            KP_ALLOC(c->d_vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns);
+            KP_ALLOC(c->d_t2, sizeof(float) * ns);
+            KP_ALLOC(c->d_t2c, sizeof(float2) * ns);
+            KP_ALLOC(c->d_c4, sizeof(double) * ns);
+            KP_ALLOC(c->d_c4r, sizeof(double) * ns);
+            KP_ALLOC(c->d_h, sizeof(float) * ns);
+            KP_ALLOC(c->d_invl2, sizeof(float) * 64);
+            KP_ALLOC(c->d_km, sizeof(float) * nimg);
+            KP_ALLOC(c->d_cnt, sizeof(int32_t) * nimg);
+            if (params->precision == KPSTM_PREC_BF16_KAHAN) KP_ALLOC(c->d_kc, sizeof(float) * nimg);
+            KP_ALLOC(c->d_cstart, sizeof(int32_t) * (s.nclass + 1));
+            KP_ALLOC(c->d_nlive, sizeof(int32_t));
+            KP_ALLOC(c->d_status, sizeof(int));
+            KP_ALLOC(c->d_hits, sizeof(unsigned long long));
+#undef KP_ALLOC
+            cudaMemcpyAsync(c->d_colxy, colxy, sizeof(float2) * ncol, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_colrow, colrow, sizeof(int32_t) * ncol, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_tilebox, box, sizeof(float4) * c->ntile, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_vrows, vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns,
+                            cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_t2, t2, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_t2c, t2c, sizeof(float2) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_c4, c4, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_c4r, c4r, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_h, hf, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_invl2, invl2, sizeof(float) * 64, cudaMemcpyHostToDevice, c->cs);
+            cudaMemsetAsync(c->d_km, 0, sizeof(float) * nimg, c->cs);
+            cudaMemsetAsync(c->d_cnt, 0, sizeof(int32_t) * nimg, c->cs);
+            if (c->d_kc) cudaMemsetAsync(c->d_kc, 0, sizeof(float) * nimg, c->cs);
+            cudaMemsetAsync(c->d_status, 0, sizeof(int), c->cs);
+            cudaMemsetAsync(c->d_hits, 0, sizeof(unsigned long long), c->cs);
+            if (cudaStreamSynchronize(c->cs) != cudaSuccess) st = KPSTM_ERR_CUDA;
+        } while (0);
+    }
+    free(colxy);
+    free(colrow);
+    free(t2);
+    free(t1);
+    free(c4);
+    free(c4r);
+    free(t2c);
+    free(hd);
+    free(hf);
+    free(box);
+    free(rowmap);
+    free(vrows);
+    if (st) {
+        kp_free_all(c);
+        return st;
+    }
+    *out = c;
+    return KPSTM_OK;
+}
+
+static int kp_free_all(kpstm_ctx *c)
+{
+    if (!c) return KPSTM_OK;
+    if (c->cs) cudaStreamSynchronize(c->cs);
+    if (c->xs) cudaStreamSynchronize(c->xs);
+    void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_c4, c->d_c4r,
+                    c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
+                    c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
+                    c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y};
+    for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
+        if (ptrs[i]) cudaFree(ptrs[i]);
+    for (int k = 0; k < 2; ++k) {
+        if (c->copy_done[k]) cudaEventDestroy(c->copy_done[k]);
+        if (c->comp_done[k]) cudaEventDestroy(c->comp_done[k]);
+    }
+    if (c->cs) cudaStreamDestroy(c->cs);
+    if (c->xs) cudaStreamDestroy(c->xs);
+    free(c);
+    return KPSTM_OK;
+}
+
+extern "C" void kpstm_destroy(kpstm_ctx *c) { kp_free_all(c); }
+
+extern "C" int kpstm_get_dims(const kpstm_ctx *c, kpstm_dims *d)
+{
+    if (!c || !d) return KPSTM_ERR_INVALID_ARG;
+    *d = c->s.dims;
+    return KPSTM_OK;
+}
+
+static int check_status(kpstm_ctx *c)
+{
+    int h = 0;
+    KP_CUDA(cudaMemcpyAsync(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    return h;
+}
+
+extern "C" int kpstm_synchronize(kpstm_ctx *c)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    return check_status(c);
+}
+
+extern "C" int kpstm_reset(kpstm_ctx *c)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    size_t nimg = (size_t)c->s.nclass * c->s.ncol * c->p.ns;
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    KP_CUDA(cudaMemsetAsync(c->d_km, 0, sizeof(float) * nimg, c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int32_t) * nimg, c->cs));
+    if (c->d_kc) KP_CUDA(cudaMemsetAsync(c->d_kc, 0, sizeof(float) * nimg, c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_hits, 0, sizeof(unsigned long long), c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_add_traces(kpstm_ctx *c, const int32_t *hdr_be, const float *samples, int64_t ntr)
+{
+    if (!c || ntr < 0 || (ntr > 0 && (!hdr_be || !samples))) return KPSTM_ERR_INVALID_ARG;
+    if (ntr == 0) return KPSTM_OK;
+    if (ntr > INT32_MAX / 2) return KPSTM_ERR_INVALID_ARG;
+    int st = grow_stage(c, ntr);
+    if (st) return st;
+    const int s = c->slot;
+    /* the copy into slot s may start once the block that last used it is imaged */
+    KP_CUDA(cudaStreamWaitEvent(c->xs, c->comp_done[s], 0));
+    KP_CUDA(cudaMemcpyAsync(c->d_hdr[s], hdr_be, sizeof(int32_t) * 60 * ntr, cudaMemcpyHostToDevice, c->xs));
+    KP_CUDA(cudaMemcpyAsync(c->d_smp[s], samples, sizeof(float) * c->p.ns * ntr, cudaMemcpyHostToDevice, c->xs));
+    KP_CUDA(cudaEventRecord(c->copy_done[s], c->xs));
+    KP_CUDA(cudaStreamWaitEvent(c->cs, c->copy_done[s], 0));
+    st = run_block(c, c->d_hdr[s], c->d_smp[s], ntr);
+    if (st) return st;
+    KP_CUDA(cudaEventRecord(c->comp_done[s], c->cs));
+    c->slot ^= 1;
+    /* the caller may reuse its buffers once they have been read */
+    KP_CUDA(cudaEventSynchronize(c->copy_done[s]));
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_add_traces_device(kpstm_ctx *c, const int32_t *d_hdr_be, const float *d_samples, int64_t ntr)
+{
+    if (!c || ntr < 0 || (ntr > 0 && (!d_hdr_be || !d_samples))) return KPSTM_ERR_INVALID_ARG;
+    if (ntr > INT32_MAX / 2) return KPSTM_ERR_INVALID_ARG;
+    return run_block(c, d_hdr_be, d_samples, ntr);
+}
+
+extern "C" int kpstm_add_segy_block(kpstm_ctx *c, const void *rec, int64_t ntr)
+{
+    if (!c || ntr < 0 || (ntr > 0 && !rec)) return KPSTM_ERR_INVALID_ARG;
+    if (ntr == 0) return KPSTM_OK;
+    if (ntr > INT32_MAX / 2) return KPSTM_ERR_INVALID_ARG;
+    int st = grow_stage(c, ntr);
+    if (st) return st;
+    const int64_t words = (60 + (int64_t)c->p.ns) * ntr;
+    if (words > c->rawcap) {
+        KP_CUDA(cudaStreamSynchronize(c->cs));
+        KP_CUDA(cudaStreamSynchronize(c->xs));
+        cudaFree(c->d_raw);
+        c->d_raw = nullptr;
+        c->rawcap = 0;
+        KP_CUDA(cudaMalloc(&c->d_raw, sizeof(uint32_t) * words));
+        c->rawcap = words;
+    }
+    const int s = c->slot;
+    KP_CUDA(cudaStreamWaitEvent(c->xs, c->comp_done[s], 0));
+    KP_CUDA(cudaStreamWaitEvent(c->xs, c->comp_done[s ^ 1], 0)); /* single raw buffer */
+    KP_CUDA(cudaMemcpyAsync(c->d_raw, rec, sizeof(uint32_t) * words, cudaMemcpyHostToDevice, c->xs));
+    KP_CUDA(cudaEventRecord(c->copy_done[s], c->xs));
+    KP_CUDA(cudaStreamWaitEvent(c->cs, c->copy_done[s], 0));
+    k_segy_decode<<<1024, 256, 0, c->cs>>>(c->d_raw, ntr, c->p.ns, c->d_hdr[s], c->d_smp[s]);
+    KP_CUDA(cudaGetLastError());
+    st = run_block(c, c->d_hdr[s], c->d_smp[s], ntr);
+    if (st) return st;
+    KP_CUDA(cudaEventRecord(c->comp_done[s], c->cs));
+    c->slot ^= 1;
+    KP_CUDA(cudaEventSynchronize(c->copy_done[s]));
+    return KPSTM_OK;
+}
+
+static int ensure_finish_scratch(kpstm_ctx *c)
+{
+    if (c->d_x) return KPSTM_OK;
+    size_t nimg = (size_t)c->s.nclass * c->s.ncol * c->p.ns;
+    KP_CUDA(cudaMalloc(&c->d_x, sizeof(float) * nimg));
+    KP_CUDA(cudaMalloc(&c->d_y, sizeof(float) * nimg));
+    return KPSTM_OK;
+}
+
+/* Finishing into device buffers out/fold ([col][cls][ns] order); either may be null. */
+static int finish_dev(kpstm_ctx *c, float *out, float *fold)
+{
+    const int ns = c->p.ns, ncol = c->s.ncol, ncls = c->s.nclass;
+    const int64_t nrows = (int64_t)ncol * ncls;
+    if (out) {
+        int st = ensure_finish_scratch(c);
+        if (st) return st;
+        k_deriv<<<1024, 256, 0, c->cs>>>(c->d_km, c->d_cnt, ncol, ncls, ns, c->p.dt, c->d_x);
+        KP_CUDA(cudaGetLastError());
+        size_t smem = sizeof(float) * (((2 * (size_t)ns + 3) & ~size_t(3)) + (size_t)ns * KP_LP_ROWS);
+        if (smem > 220 * 1024) return KPSTM_ERR_UNSUPPORTED;
+        KP_CUDA(cudaFuncSetAttribute(k_lowpass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_lowpass<<<(unsigned)((nrows + KP_LP_ROWS - 1) / KP_LP_ROWS), 256, smem, c->cs>>>(c->d_x, c->d_h, nrows,
+                                                                                          ns, out);
+        KP_CUDA(cudaGetLastError());
+    }
+    if (fold) {
+        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, ncol, ncls, ns, fold);
+        KP_CUDA(cudaGetLastError());
+    }
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_finish_device(kpstm_ctx *c, float *d_out, float *d_fold)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    int st = finish_dev(c, d_out, d_fold);
+    if (st) return st;
+    return check_status(c);
+}
+
+extern "C" int kpstm_finish(kpstm_ctx *c, float *out, float *fold)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    int st = ensure_finish_scratch(c);
+    if (st) return st;
+    const size_t bytes = sizeof(float) * (size_t)c->s.dims.out_elems;
+    if (out) {
+        st = finish_dev(c, c->d_y, nullptr);
+        if (st) return st;
+        KP_CUDA(cudaMemcpyAsync(out, c->d_y, bytes, cudaMemcpyDeviceToHost, c->cs));
+    }
+    if (fold) {
+        /* d_x is free again once the low-pass has read it (stream order) */
+        st = finish_dev(c, nullptr, c->d_x);
+        if (st) return st;
+        KP_CUDA(cudaMemcpyAsync(fold, c->d_x, bytes, cudaMemcpyDeviceToHost, c->cs));
+    }
+    return check_status(c);
+}
+
+extern "C" int kpstm_get_accumulators(kpstm_ctx *c, float *km, float *fold)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->xs));
+    int st = ensure_finish_scratch(c);
+    if (st) return st;
+    const int ns = c->p.ns, ncol = c->s.ncol, ncls = c->s.nclass;
+    const size_t bytes = sizeof(float) * (size_t)c->s.dims.out_elems;
+    if (km) {
+        k_relayout<<<1024, 256, 0, c->cs>>>(c->d_km, nullptr, ncol, ncls, ns, c->d_x);
+        KP_CUDA(cudaGetLastError());
+        KP_CUDA(cudaMemcpyAsync(km, c->d_x, bytes, cudaMemcpyDeviceToHost, c->cs));
+    }
+    if (fold) {
+        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, ncol, ncls, ns, c->d_y);
+        KP_CUDA(cudaGetLastError());
+        KP_CUDA(cudaMemcpyAsync(fold, c->d_y, bytes, cudaMemcpyDeviceToHost, c->cs));
+    }
+    return check_status(c);
+}
+
+extern "C" int kpstm_pair_count(const kpstm_ctx *c, int64_t *pairs)
+{
+    if (!c || !pairs) return KPSTM_ERR_INVALID_ARG;
+    unsigned long long h = 0;
+    KP_CUDA(cudaMemcpyAsync(&h, c->d_hits, sizeof(h), cudaMemcpyDeviceToHost, c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    *pairs = (int64_t)h * c->p.ns;
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_write_su(const kpstm_ctx *c, const float *image, void *dst, int64_t dst_bytes)
+{
+    if (!c || !image || !dst) return KPSTM_ERR_INVALID_ARG;
+    const int ns = c->p.ns, ncls = c->s.nclass, ncol = c->s.ncol;
+    const int64_t rec = 240 + 4 * (int64_t)ns;
+    const int64_t ntrace = (int64_t)ncol * ncls;
+    if (dst_bytes < ntrace * rec) return KPSTM_ERR_INVALID_ARG;
+    uint8_t *o = (uint8_t *)dst;
+    int64_t tracl = (int64_t)ncol * ncls * c->p.job_id + 1;
+    for (int col = 0; col < ncol; ++col) {
+        for (int cls = 0; cls < ncls; ++cls) {
+            uint8_t *r = o + ((int64_t)col * ncls + cls) * rec;
+            kpstm_su_headers(&c->p, &c->s, col, cls, tracl++, r);
+            const float *d = image + ((int64_t)col * ncls + cls) * ns;
+            for (int t = 0; t < ns; ++t) {
+                uint32_t u;
+                memcpy(&u, &d[t], 4);
+                r[240 + 4 * t + 0] = (uint8_t)(u >> 24);
+                r[240 + 4 * t + 1] = (uint8_t)(u >> 16);
+                r[240 + 4 * t + 2] = (uint8_t)(u >> 8);
+                r[240 + 4 * t + 3] = (uint8_t)u;
+            }
+        }
+    }
+    return KPSTM_OK;
+}

@@ -1,0 +1,577 @@
+/*
+ * Kernels of libkpstm (sm_103a).
+ *
+ *  k_segy_decode   raw SEG-Y records -> header words + IEEE samples
+ *                  (Kirchhoff.c:1280-1290)
+ *  k_geometry      trace geometry, offset class, slab cull (:1297-1338)
+ *  k_bucket        stable partition of the block's traces by class
+ *  k_prep          per-trace double running integral (:1312-1328) and the
+ *                  tap table the imaging kernel gathers from
+ *  k_image         imaging (:1341-1403) as a gather: a CTA owns 8 image
+ *                  columns x a time window of one offset class in registers
+ *                  and streams that class's traces through shared memory
+ *                  with TMA bulk copies, in trace order
+ *  k_deriv / k_lowpass / k_relayout   finishing (:1440-1479)
+ */
+#ifndef KPSTM_KERNELS_CUH
+#define KPSTM_KERNELS_CUH
+
+#include "kpstm_device.cuh"
+
+#define KP_TB_REF 4     /* traces per staged batch, reference mode */
+#define KP_TB_FULL 2    /* traces per staged batch, full mode */
+#define KP_LCH 1024     /* traces examined per compaction chunk */
+#define KP_THREADS 256  /* 8 warps = KPSTM_COLS_PER_CTA columns */
+
+struct KpGeomArgs {
+    const int32_t *hdr_be; /* [ntr][60] */
+    int64_t ntr;
+    kpstm_geom *geom;      /* [ntr], block order */
+    int32_t *cls;          /* [ntr] */
+    int *status;
+    double ox, oy, xy_scale, oh, dh, cull_radius;
+    float sinA, cosA, IXc, IYc;
+    int nh, stack;
+};
+
+struct KpPrepArgs {
+    const float *samples;          /* [ntr][ns], fp32 */
+    const uint16_t *samples_bf16;  /* [ntr][ns], bf16 (precision mode) or null */
+    const float *scale;            /* [ntr] per-trace scale for bf16 */
+    const kpstm_geom *geom_raw;    /* [ntr] block order */
+    const int32_t *order;          /* [nslot] slot -> trace */
+    const int32_t *nlive;          /* device scalar */
+    kpstm_geom *geom;              /* [nslot] slot order */
+    float *table;                  /* [nslot][row] */
+    const double *c4;              /* [ns] 4*t2[t] */
+    const double *c4r;             /* [ns] RN(1/(4*t2[t])) */
+    int64_t row;                   /* floats per table row */
+    int ns, tm, full;
+    float dt;
+};
+
+struct KpImageArgs {
+    const kpstm_geom *geom;        /* slot order */
+    const int32_t *class_start;    /* [ncls+1] */
+    const float *table;            /* [nslot][row] */
+    int64_t row;
+    const float2 *colxy;           /* [ncol] */
+    const int32_t *colrow;         /* [ncol] compact velocity row, -1 = below grid */
+    const float4 *tilebox;         /* [ntile] xmin, xmax, ymin, ymax */
+    const float2 *vrows;           /* [nrow][ns] {v^2, RN(1/v^2)} */
+    const float *t2;               /* [ns] reference t2 */
+    const float2 *t2c;             /* [ns] full mode {(t dt/2)^2, t dt/8} */
+    const float *inv_l2;           /* [lmax+1] 1/L^2 */
+    float *km;                     /* [ncls][ncol][ns] */
+    float *kc;                     /* Kahan compensation, same layout, or null */
+    int32_t *cnt;                  /* [ncls][ncol][ns] fold - 1 */
+    unsigned long long *hits;      /* (trace, column) pairs in aperture */
+    int *status;
+    int ncol, ns, tm, lmax;
+    float dt, rdt, nsf, lmaxf;
+    double aperture;
+    float tile_r2;                 /* squared tile-test radius (aperture + margin) */
+    float aax, aay;                /* full mode: line spacing / dt */
+};
+
+/* ------------------------------------------------------------------------ */
+
+__global__ void k_segy_decode(const uint32_t *rec, int64_t ntr, int ns, int32_t *hdr, float *samples)
+{
+    const int64_t words = 60 + (int64_t)ns;
+    const int64_t n = ntr * words;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t tr = i / words, k = i - tr * words;
+        uint32_t u = rec[i];
+        if (k < 60) {
+            hdr[tr * 60 + k] = (int32_t)u; /* kept big-endian, as read */
+        } else {
+            int32_t w = (int32_t)__byte_perm(u, 0, 0x0123);
+            int s = (((w >> 31) & 0x01) * (-2)) + 1;
+            float frac = __fdiv_rn(__int2float_rn(w & 0x00ffffff), 16777216.0f);
+            float scale = ldexpf(1.0f, 4 * (((w >> 24) & 0x7f) - 64));
+            samples[tr * ns + (k - 60)] = __fmul_rn(__fmul_rn(__int2float_rn(s), frac), scale);
+        }
+    }
+}
+
+__device__ __forceinline__ int kp_coord(const KpGeomArgs &a, uint32_t w_be, double o, bool *ok)
+{
+    uint32_t u = __byte_perm(w_be, 0, 0x0123);
+    double v = (double)u - (a.xy_scale == 1.0 ? o : o / a.xy_scale);
+    if (!(v > -2147483649.0 && v < 2147483648.0)) {
+        *ok = false;
+        return 0;
+    }
+    return (int)v; /* truncation, as the assignment to int i at Kirchhoff.c:1297 */
+}
+
+/* Kirchhoff.c:1297-1310 and the slab cull of :1332-1338. */
+__global__ void k_geometry(KpGeomArgs a)
+{
+    int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (it >= a.ntr) return;
+    const uint32_t *h = (const uint32_t *)a.hdr_be + it * 60;
+    bool ok = true;
+    int si = kp_coord(a, h[18], a.ox, &ok), sj = kp_coord(a, h[19], a.oy, &ok);
+    int gi = kp_coord(a, h[20], a.ox, &ok), gj = kp_coord(a, h[21], a.oy, &ok);
+    kpstm_geom g;
+    if (a.xy_scale == 1.0) {
+        g.sxt = __fadd_rn(__fmul_rn(a.cosA, __int2float_rn(si)), __fmul_rn(a.sinA, __int2float_rn(sj)));
+        g.syt = __fadd_rn(__fmul_rn(-a.sinA, __int2float_rn(si)), __fmul_rn(a.cosA, __int2float_rn(sj)));
+        g.gxt = __fadd_rn(__fmul_rn(a.cosA, __int2float_rn(gi)), __fmul_rn(a.sinA, __int2float_rn(gj)));
+        g.gyt = __fadd_rn(__fmul_rn(-a.sinA, __int2float_rn(gi)), __fmul_rn(a.cosA, __int2float_rn(gj)));
+    } else { /* Kirchhoff_GHTest1.c:1302-1312: float products scaled in double */
+        const double s = a.xy_scale;
+        g.sxt = (float)((double)__fmul_rn(a.cosA, __int2float_rn(si)) * s + (double)__fmul_rn(a.sinA, __int2float_rn(sj)) * s);
+        g.syt = (float)((double)__fmul_rn(-a.sinA, __int2float_rn(si)) * s + (double)__fmul_rn(a.cosA, __int2float_rn(sj)) * s);
+        g.gxt = (float)((double)__fmul_rn(a.cosA, __int2float_rn(gi)) * s + (double)__fmul_rn(a.sinA, __int2float_rn(gj)) * s);
+        g.gyt = (float)((double)__fmul_rn(-a.sinA, __int2float_rn(gi)) * s + (double)__fmul_rn(a.cosA, __int2float_rn(gj)) * s);
+    }
+    float dx = __fsub_rn(g.sxt, g.gxt), dy = __fsub_rn(g.syt, g.gyt);
+    float h2 = (float)(0.25 * (double)__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    g.cmpx = (float)(0.5 * (double)__fadd_rn(g.sxt, g.gxt));
+    g.cmpy = (float)(0.5 * (double)__fadd_rn(g.syt, g.gyt));
+    double offd = floor(__ddiv_rn(__dsub_rn(__dmul_rn(2.0, __dsqrt_rn((double)h2)), a.oh), a.dh));
+    int off = (offd > -2147483648.0 && offd < 2147483647.0) ? (int)offd : -1;
+    bool valid = off >= 0 && off < a.nh;
+    float cx = __fsub_rn(a.IXc, g.cmpx), cy = __fsub_rn(a.IYc, g.cmpy);
+    float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
+    bool live = valid && ((double)dIC < a.cull_radius);
+    g.cls = live ? (a.stack ? 0 : off) : -1;
+    g.src = (int32_t)it;
+    if (!ok) {
+        g.cls = -1;
+        kp_fail(a.status, KPSTM_ERR_GEOMETRY);
+    }
+    a.geom[it] = g;
+    a.cls[it] = g.cls;
+}
+
+/* Stable partition of the block by class (single CTA): class_start[c] is
+   the first slot of class c, order[slot] the trace, in block order within a
+   class - so the gather visits a class's traces in the reference's order. */
+__global__ void __launch_bounds__(1024) k_bucket(const int32_t *cls, int64_t ntr, int ncls,
+                                                 int32_t *class_start, int32_t *order, int32_t *nlive)
+{
+    extern __shared__ int32_t hist[]; /* [ncls + 1] */
+    for (int c = threadIdx.x; c <= ncls; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < ntr; i += blockDim.x) {
+        int c = cls[i];
+        if (c >= 0) atomicAdd(&hist[c], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int c = 0; c < ncls; ++c) {
+            int n = hist[c];
+            hist[c] = run;
+            class_start[c] = run;
+            run += n;
+        }
+        class_start[ncls] = run;
+        *nlive = run;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    for (int64_t base = 0; base < ntr; base += 32) {
+        int64_t i = base + lane;
+        int c = i < ntr ? cls[i] : -1;
+        unsigned peers = __match_any_sync(0xffffffffu, c);
+        int rank = __popc(peers & ((1u << lane) - 1u));
+        int pos = 0;
+        if (c >= 0) pos = hist[c] + rank;
+        __syncwarp();
+        if (c >= 0) {
+            order[pos] = (int32_t)i;
+            if (rank == 0) hist[c] += __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+/* Per-trace running integrals of Kirchhoff.c:1312-1328, one thread per
+   trace, in the reference's order and precision: the first integral adds
+   f[t]/(4*t2[t]) in double and stores float, the tail adds
+   f[ns-1]/(dt*dt*t*t) in float (the fast-math a/(b*c) form of
+   :1320), the second integral is a float running sum, the front is
+   mirrored.  Reference mode stores D[T] = -2P[T] + P[T-2] + P[T+2] summed in
+   double (:1391-1392); full mode stores P over [-tm, ns+tm-2) as pairs
+   {P[i], P[i+1]-P[i]} for linear interpolation. */
+__global__ void k_prep(KpPrepArgs a)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= *a.nlive) return;
+    const int32_t src = a.order[i];
+    kpstm_geom g = a.geom_raw[src];
+    a.geom[i] = g;
+    const int ns = a.ns, tm = a.tm;
+    float *row = a.table + i * a.row;
+    const float *f32 = a.samples ? a.samples + (int64_t)src * ns : nullptr;
+    const uint16_t *f16 = a.samples_bf16 ? a.samples_bf16 + (int64_t)src * ns : nullptr;
+    const float sc = f16 ? a.scale[src] : 1.0f;
+#define KP_SAMPLE(t) (f32 ? f32[(t)] : __fmul_rn(__uint_as_float(((uint32_t)f16[(t)]) << 16), sc))
+    const float flast = KP_SAMPLE(ns - 1);
+    const float dt2 = __fmul_rn(a.dt, a.dt);
+    float p1 = KP_SAMPLE(0);
+    float p2 = p1;
+    /* ring of P2[t-4..t] for the reference taps; P2[1], P2[2] kept for the mirror */
+    float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, r4 = p2;
+    float m1 = 0.f, m2 = 0.f;
+    const int tend = a.full ? ns + tm - 2 : ns + 2;
+    float2 *q = reinterpret_cast<float2 *>(row);
+    float prev = p2;
+    for (int t = 1; t < tend; ++t) {
+        if (t < ns) {
+            double v = __dadd_rn((double)p1, kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]));
+            p1 = __double2float_rn(v);
+        } else {
+            float tf = __int2float_rn(t);
+            p1 = __fadd_rn(p1, __fdiv_rn(flast, __fmul_rn(__fmul_rn(dt2, tf), tf)));
+        }
+        p2 = __fadd_rn(p2, p1);
+        if (t == 1) m1 = p2;
+        if (t == 2) m2 = p2;
+        if (!a.full) {
+            r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = p2; /* r4 = P2[t] */
+            if (t >= 2) {
+                int T = t - 2;
+                float pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
+                double d = __dadd_rn(__dadd_rn(-2.0 * (double)r2, (double)pm), (double)r4);
+                if (T < ns) row[T] = __double2float_rn(d);
+            }
+        } else {
+            q[t - 1 + tm] = make_float2(prev, __fsub_rn(p2, prev)); /* entry for P2[t-1] */
+            prev = p2;
+        }
+    }
+    if (a.full) {
+        /* entries for P2[-j], j = 1..tm: {P2[j], P2[j-1] - P2[j]} */
+        for (int j = 1; j <= tm; ++j) {
+            float pj = q[j + tm].x, pj1 = q[j - 1 + tm].x;
+            q[tm - j] = make_float2(pj, __fsub_rn(pj1, pj));
+        }
+    }
+#undef KP_SAMPLE
+}
+
+/* ------------------------------------------------------------------------ */
+/* Imaging.  Grid (ntile, ncls, nwin); block 256 = 8 warps; warp w owns image
+   column blockIdx.x*8 + w, lane l owns samples tw0 + l + 32k, k < K. */
+
+__device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float cy, float r2)
+{
+    float dx = fmaxf(fmaxf(box.x - cx, cx - box.y), 0.0f);
+    float dy = fmaxf(fmaxf(box.z - cy, cy - box.w), 0.0f);
+    return dx * dx + dy * dy < r2;
+}
+
+template <int K, bool FULL, bool KAHAN>
+__global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
+{
+    constexpr int W = 32 * K;
+    constexpr int TB = FULL ? KP_TB_FULL : KP_TB_REF;
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int cls = blockIdx.y;
+    const int tw0 = blockIdx.z * W;
+    const int col = blockIdx.x * KPSTM_COLS_PER_CTA + w;
+    const bool colok = col < a.ncol;
+    const int ns = a.ns;
+    const int64_t row = a.row;
+
+    /* shared layout */
+    uint8_t *p = smem;
+    float2 *s_v = reinterpret_cast<float2 *>(p);                 /* ref: [8][W] {v2, rv2}; full: rv2 in .y */
+    p += sizeof(float2) * KPSTM_COLS_PER_CTA * W;
+    float2 *s_t = reinterpret_cast<float2 *>(p);                 /* [W] ref {t2,0} / full {t2, t0/8} */
+    p += sizeof(float2) * W;
+    float *s_buf = reinterpret_cast<float *>(p);                 /* [2][TB][row] */
+    p += sizeof(float) * 2 * TB * row;
+    int32_t *s_list = reinterpret_cast<int32_t *>(p);            /* [KP_LCH] */
+    p += sizeof(int32_t) * KP_LCH;
+    int32_t *s_wsum = reinterpret_cast<int32_t *>(p);            /* [8] */
+    p += sizeof(int32_t) * 8;
+    int32_t *s_flag = reinterpret_cast<int32_t *>(p);            /* [2]: abort, hits */
+    p += sizeof(int32_t) * 2;
+    p = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
+    uint64_t *s_bar = reinterpret_cast<uint64_t *>(p);           /* [2] */
+
+    const int vrow = colok ? a.colrow[col] : -1;
+    for (int t = lane; t < W; t += 32) {
+        int tt = tw0 + t;
+        float2 v = make_float2(1.0f, 1.0f);
+        if (vrow >= 0 && tt < ns) v = a.vrows[(int64_t)vrow * ns + tt];
+        s_v[w * W + t] = v;
+    }
+    for (int t = tid; t < W; t += KP_THREADS) {
+        int tt = tw0 + t;
+        float2 v = make_float2(0.0f, 0.0f);
+        if (tt < ns) v = FULL ? a.t2c[tt] : make_float2(a.t2[tt], 0.0f);
+        s_t[t] = v;
+    }
+    if (tid == 0) {
+        kp_mbar_init(&s_bar[0], 1);
+        kp_mbar_init(&s_bar[1], 1);
+        s_flag[0] = 0;
+        s_flag[1] = 0;
+        kp_fence_mbar_init();
+    }
+    const float2 cxy = colok ? a.colxy[col] : make_float2(0.f, 0.f);
+    const float IX = cxy.x, IY = cxy.y;
+    const float4 box = a.tilebox[blockIdx.x];
+    const int64_t obase = ((int64_t)cls * a.ncol + (colok ? col : 0)) * ns + tw0 + lane;
+
+    float acc[K], comp[KAHAN ? K : 1];
+    int cnt[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        int tt = tw0 + lane + 32 * k;
+        acc[k] = (colok && tt < ns) ? a.km[obase + 32 * k] : 0.0f;
+        if (KAHAN) comp[k] = (colok && tt < ns) ? a.kc[obase + 32 * k] : 0.0f;
+        cnt[k] = 0;
+    }
+    __syncthreads();
+
+    const int cb = a.class_start[cls], ce = a.class_start[cls + 1];
+    const uint32_t row_bytes = (uint32_t)(row * sizeof(float));
+    uint32_t nb = 0; /* batches issued so far (buffer = nb & 1) */
+    int my_hits = 0;
+    bool abort = false;
+
+    for (int c0 = cb; c0 < ce && !abort; c0 += KP_LCH) {
+        /* order-preserving compaction of the chunk's traces that can reach
+           any column of this tile */
+        int n = 0;
+        for (int r = 0; r < KP_LCH / KP_THREADS; ++r) {
+            int i = c0 + r * KP_THREADS + tid;
+            bool pass = false;
+            if (i < ce) {
+                const kpstm_geom &g = a.geom[i];
+                pass = kp_tile_test(box, g.cmpx, g.cmpy, a.tile_r2);
+            }
+            unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (lane == 0) s_wsum[w] = __popc(m);
+            __syncthreads();
+            int before = 0, total = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                int v = s_wsum[q];
+                before += q < w ? v : 0;
+                total += v;
+            }
+            if (pass) s_list[n + before + __popc(m & ((1u << lane) - 1u))] = i;
+            n += total;
+            __syncthreads();
+        }
+        const int nbatch = (n + TB - 1) / TB;
+        auto issue = [&](int b, uint32_t slot) {
+            int j0 = b * TB, j1 = min(n, j0 + TB);
+            uint64_t *bar = &s_bar[slot & 1];
+            kp_fence_proxy_async();
+            kp_mbar_expect_tx(bar, (uint32_t)(j1 - j0) * row_bytes);
+            for (int j = j0; j < j1; ++j)
+                kp_bulk_g2s(s_buf + ((slot & 1) * TB + (j - j0)) * row, a.table + (int64_t)s_list[j] * row,
+                            row_bytes, bar);
+        };
+        if (tid == 0 && nbatch > 0) issue(0, nb);
+        for (int b = 0; b < nbatch; ++b, ++nb) {
+            const bool next = b + 1 < nbatch;
+            if (tid == 0 && next) issue(b + 1, nb + 1);
+            if (!kp_mbar_wait(&s_bar[nb & 1], (nb >> 1) & 1)) {
+                s_flag[0] = 1;
+                kp_fail(a.status, KPSTM_ERR_TIMEOUT);
+                /* do not leave with our next copy still landing in shared memory */
+                if (tid == 0 && next) kp_mbar_wait(&s_bar[(nb + 1) & 1], ((nb + 1) >> 1) & 1);
+            }
+            if (s_flag[0] == 0 && colok) {
+                const int j0 = b * TB, j1 = min(n, j0 + TB);
+                for (int j = j0; j < j1; ++j) {
+                    const kpstm_geom g = a.geom[s_list[j]];
+                    float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
+                    float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
+                    if (!((double)dIC < a.aperture)) continue; /* Kirchhoff.c:1352-1354, warp-uniform */
+                    if (vrow < 0) {
+                        kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
+                        continue;
+                    }
+                    ++my_hits;
+                    float sx = __fsub_rn(IX, g.sxt), sy = __fsub_rn(IY, g.syt);
+                    float gx = __fsub_rn(IX, g.gxt), gy = __fsub_rn(IY, g.gyt);
+                    const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
+                    const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
+                    const float *tab = s_buf + ((nb & 1) * TB + (j - j0)) * row;
+                    const float2 *sv = s_v + w * W + lane;
+                    const float2 *st = s_t + lane;
+                    if (!FULL) {
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            const float2 vr = sv[32 * k];
+                            const float t2 = st[32 * k].x;
+                            float s1 = __fadd_rn(t2, kp_div_rn(dIS2, vr.x, vr.y));
+                            float s2 = __fadd_rn(t2, kp_div_rn(dIR2, vr.x, vr.y));
+                            float S = kp_dsqrt_sum(s1, s2);
+                            float qq = kp_div_rn(S, a.dt, a.rdt); /* dsr/dt, :1384 */
+                            if (qq < a.nsf) {                    /* T < ns, :1387 */
+                                int T = kp_floor_bits(qq) - KP_MAGIC_BITS;
+                                float d = tab[T];
+                                if (KAHAN) {
+                                    float y = __fsub_rn(d, comp[k]);
+                                    float s = __fadd_rn(acc[k], y);
+                                    comp[k] = __fsub_rn(__fsub_rn(s, acc[k]), y);
+                                    acc[k] = s;
+                                } else {
+                                    acc[k] = __fadd_rn(acc[k], d);
+                                }
+                                cnt[k] += 1;
+                            }
+                        }
+                    } else {
+                        /* full physics: tau = ts + tr, ts = sqrt(t0^2/4 + |I-S|^2/v^2);
+                           a triangle of real half-width Lf (1 + the operator's lateral
+                           slope in samples per trace spacing, <= lmax) read from the
+                           double running integral at three fractional positions;
+                           weight t0 (1/ts + 1/tr)^2 / 8 */
+                        const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
+                        const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
+                        /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm */
+                        const float2 *q2 = reinterpret_cast<const float2 *>(tab) + a.tm;
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            const float rv2 = sv[32 * k].y;
+                            const float2 tc = st[32 * k];
+                            float as = fmaxf(fmaf(dIS2, rv2, tc.x), 1e-30f);
+                            float ar = fmaxf(fmaf(dIR2, rv2, tc.x), 1e-30f);
+                            float rs = kp_rsqrt_approx(as), rr = kp_rsqrt_approx(ar);
+                            float Tf = fmaf(as, rs, ar * rr) * a.rdt;
+                            if (Tf < a.nsf - 1.0f) {
+                                float gxx = fmaf(axs, rs, axr * rr), gyy = fmaf(ays, rs, ayr * rr);
+                                float Lf = fminf(fmaf(fabsf(gxx) + fabsf(gyy), rv2, 1.0f), a.lmaxf);
+                                float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
+                                int b0 = kp_floor_bits(x0), ba = kp_floor_bits(xa), bb = kp_floor_bits(xb);
+                                float f0 = x0 - (__int_as_float(b0) - KP_MAGIC);
+                                float fa = xa - (__int_as_float(ba) - KP_MAGIC);
+                                float fb = xb - (__int_as_float(bb) - KP_MAGIC);
+                                float2 q0 = q2[b0 - KP_MAGIC_BITS], qa = q2[ba - KP_MAGIC_BITS], qb = q2[bb - KP_MAGIC_BITS];
+                                /* second difference without cancellation: table
+                                   differences (exact for neighbouring values) plus the
+                                   small interpolation terms */
+                                float big = (qa.x - q0.x) + (qb.x - q0.x);
+                                float small = fmaf(-2.0f * f0, q0.y, fmaf(fa, qa.y, fb * qb.y));
+                                float il = kp_rcp_approx(Lf);
+                                float tri = (big + small) * (il * il);
+                                float u = rs + rr;
+                                float wgt = tc.y * u * u;
+                                if (KAHAN) {
+                                    float y = fmaf(wgt, tri, -comp[k]);
+                                    float s = acc[k] + y;
+                                    comp[k] = (s - acc[k]) - y;
+                                    acc[k] = s;
+                                } else {
+                                    acc[k] = fmaf(wgt, tri, acc[k]);
+                                }
+                                cnt[k] += 1;
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            if (s_flag[0]) {
+                abort = true;
+                break;
+            }
+        }
+    }
+    if (abort) return;
+    if (colok) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            int tt = tw0 + lane + 32 * k;
+            if (tt < ns) {
+                a.km[obase + 32 * k] = acc[k];
+                if (KAHAN) a.kc[obase + 32 * k] = comp[k];
+                a.cnt[obase + 32 * k] += cnt[k];
+            }
+        }
+    }
+    if (blockIdx.z == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Finishing, Kirchhoff.c:1457-1462: x[t] = -dt*t*(km[t]-km[t-1])*dt/fold[t]
+   in float, x[0] = 0; rows written in output order [col][cls]. */
+__global__ void k_deriv(const float *km, const int32_t *cnt, int ncol, int ncls, int ns, float dt, float *x)
+{
+    const int64_t n = (int64_t)ncls * ncol * ns;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = i / ns;
+        int t = (int)(i - r * ns);
+        int cls = (int)(r / ncol), col = (int)(r - (int64_t)cls * ncol);
+        float v = 0.0f;
+        if (t > 0) {
+            float fold = __int2float_rn(cnt[i] + 1);
+            v = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(-dt, __int2float_rn(t)), __fsub_rn(km[i], km[i - 1])), dt), fold);
+        }
+        x[((int64_t)col * ncls + cls) * ns + t] = v;
+    }
+}
+
+/* Low-pass of Kirchhoff.c:1465-1479 as the equivalent circular convolution
+   y = x (*) h (h real and even, from the anti-alias spectrum); y[0] = 0.
+   A CTA convolves 8 rows; h is held twice in shared memory so that
+   h[(t - j) mod ns] = hh[t - j + ns]. */
+#define KP_LP_ROWS 8
+__global__ void __launch_bounds__(256) k_lowpass(const float *x, const float *h, int64_t nrows, int ns, float *y)
+{
+    extern __shared__ __align__(16) float lp[];
+    const int hn = (2 * ns + 3) & ~3; /* keeps xs 16-byte aligned for the float4 reads */
+    float *hh = lp;                   /* [2*ns] */
+    float *xs = lp + hn;              /* [ns][KP_LP_ROWS], row-interleaved */
+    const int64_t r0 = (int64_t)blockIdx.x * KP_LP_ROWS;
+    for (int i = threadIdx.x; i < 2 * ns; i += blockDim.x) hh[i] = h[i < ns ? i : i - ns];
+    for (int i = threadIdx.x; i < ns * KP_LP_ROWS; i += blockDim.x) {
+        int r = i / ns, j = i - r * ns;
+        xs[j * KP_LP_ROWS + r] = (r0 + r < nrows) ? x[(r0 + r) * ns + j] : 0.0f;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ns; t += blockDim.x) {
+        float acc[KP_LP_ROWS];
+#pragma unroll
+        for (int r = 0; r < KP_LP_ROWS; ++r) acc[r] = 0.0f;
+        const float *hp = hh + t + ns;
+        for (int j = 0; j < ns; ++j) {
+            float hv = hp[-j];
+            float4 xa = *reinterpret_cast<const float4 *>(xs + j * KP_LP_ROWS);
+            float4 xb = *reinterpret_cast<const float4 *>(xs + j * KP_LP_ROWS + 4);
+            acc[0] = fmaf(xa.x, hv, acc[0]);
+            acc[1] = fmaf(xa.y, hv, acc[1]);
+            acc[2] = fmaf(xa.z, hv, acc[2]);
+            acc[3] = fmaf(xa.w, hv, acc[3]);
+            acc[4] = fmaf(xb.x, hv, acc[4]);
+            acc[5] = fmaf(xb.y, hv, acc[5]);
+            acc[6] = fmaf(xb.z, hv, acc[6]);
+            acc[7] = fmaf(xb.w, hv, acc[7]);
+        }
+#pragma unroll
+        for (int r = 0; r < KP_LP_ROWS; ++r)
+            if (r0 + r < nrows) y[(r0 + r) * ns + t] = t == 0 ? 0.0f : acc[r];
+    }
+}
+
+/* [cls][col][ns] -> [col][cls][ns]; fold = 1 + count when cnt is given. */
+__global__ void k_relayout(const float *src, const int32_t *cnt, int ncol, int ncls, int ns, float *dst)
+{
+    const int64_t n = (int64_t)ncls * ncol * ns;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = i / ns;
+        int t = (int)(i - r * ns);
+        int cls = (int)(r / ncol), col = (int)(r - (int64_t)cls * ncol);
+        float v = cnt ? __int2float_rn(cnt[i] + 1) : src[i];
+        dst[((int64_t)col * ncls + cls) * ns + t] = v;
+    }
+}
+
+#endif

@@ -1,0 +1,132 @@
+"""Python front end of libkpstm (ctypes over include/kpstm.h).
+
+``Migration`` is one imaging job - the reference's ``kirchhoff(job_id)``
+(Kirchhoff.c:1104) with its set-up (main :263-331): create it with the
+job's parameters and v_rms model, feed trace blocks in file order (one
+``ntblock`` read of Kirchhoff.c:1276-1290 per call), then ``finish()``
+returns the finished image [nx, ny, nh, ns] as the reference writes it
+(:1440-1479).  Every call goes to the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi, segy
+
+
+class Migration:
+    def __init__(self, params: dict, velocity):
+        self._lib = capi.load()
+        self.params = dict(params)
+        prm = capi.make_params(self.params)
+        vel, keep = capi.make_velocity(velocity)
+        h = C.c_void_p()
+        capi.check("kpstm_create", self._lib.kpstm_create(C.byref(prm), C.byref(vel), C.byref(h)))
+        del keep
+        self._h = h
+        d = capi.KpstmDims()
+        capi.check("kpstm_get_dims", self._lib.kpstm_get_dims(self._h, C.byref(d)))
+        self.dims = {f: getattr(d, f) for f, _ in capi.KpstmDims._fields_}
+        self.shape = (d.nx, d.ny, d.nh, d.ns)
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.kpstm_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- traces ---------------------------------------------------------------
+    def add_traces(self, headers: np.ndarray, samples: np.ndarray, headers_are_be: bool = False) -> None:
+        """headers: [ntr, 60] int32 header words (host order unless
+        ``headers_are_be``); samples: [ntr, ns] float32."""
+        hdr = np.ascontiguousarray(headers if headers_are_be else segy.headers_be(headers), dtype=np.int32)
+        smp = np.ascontiguousarray(samples, dtype=np.float32)
+        ntr = smp.shape[0]
+        if hdr.shape != (ntr, 60) or smp.shape[1] != self.shape[3]:
+            raise ValueError("headers/samples shape mismatch")
+        capi.check("kpstm_add_traces",
+                   self._lib.kpstm_add_traces(self._h, hdr.ctypes.data, smp.ctypes.data, ntr))
+
+    def add_traces_ptr(self, hdr_be_ptr: int, samples_ptr: int, ntr: int) -> None:
+        """Host pointers (e.g. pinned buffers) to BE header words and samples."""
+        capi.check("kpstm_add_traces", self._lib.kpstm_add_traces(self._h, hdr_be_ptr, samples_ptr, ntr))
+
+    def add_traces_device(self, d_hdr_be: int, d_samples: int, ntr: int) -> None:
+        """Device pointers; the work is queued on the context's stream."""
+        capi.check("kpstm_add_traces_device",
+                   self._lib.kpstm_add_traces_device(self._h, d_hdr_be, d_samples, ntr))
+
+    def add_segy_block(self, records: np.ndarray) -> None:
+        """records: uint8 [ntr, 240 + 4*ns] raw SEG-Y trace records (IBM floats)."""
+        rec = np.ascontiguousarray(records, dtype=np.uint8)
+        capi.check("kpstm_add_segy_block", self._lib.kpstm_add_segy_block(self._h, rec.ctypes.data, rec.shape[0]))
+
+    # -- results --------------------------------------------------------------
+    def finish(self, want_fold: bool = False):
+        out = np.empty(self.shape, np.float32)
+        fold = np.empty(self.shape, np.float32) if want_fold else None
+        capi.check("kpstm_finish", self._lib.kpstm_finish(
+            self._h, out.ctypes.data, None if fold is None else fold.ctypes.data))
+        return (out, fold) if want_fold else out
+
+    def finish_ptr(self, out_ptr: int, fold_ptr: int | None = None) -> None:
+        capi.check("kpstm_finish", self._lib.kpstm_finish(self._h, out_ptr, fold_ptr))
+
+    def finish_device(self, d_out: int, d_fold: int | None = None) -> None:
+        capi.check("kpstm_finish_device", self._lib.kpstm_finish_device(self._h, d_out, d_fold))
+
+    def accumulators(self):
+        km = np.empty(self.shape, np.float32)
+        fold = np.empty(self.shape, np.float32)
+        capi.check("kpstm_get_accumulators",
+                   self._lib.kpstm_get_accumulators(self._h, km.ctypes.data, fold.ctypes.data))
+        return km, fold
+
+    def pairs(self) -> int:
+        v = C.c_int64()
+        capi.check("kpstm_pair_count", self._lib.kpstm_pair_count(self._h, C.byref(v)))
+        return v.value
+
+    def synchronize(self) -> None:
+        capi.check("kpstm_synchronize", self._lib.kpstm_synchronize(self._h))
+
+    def reset(self) -> None:
+        capi.check("kpstm_reset", self._lib.kpstm_reset(self._h))
+
+    def write_su(self, image: np.ndarray) -> bytes:
+        ns = self.shape[3]
+        n = self.shape[0] * self.shape[1] * self.shape[2]
+        buf = np.empty(n * (240 + 4 * ns), np.uint8)
+        img = np.ascontiguousarray(image, np.float32)
+        capi.check("kpstm_write_su", self._lib.kpstm_write_su(self._h, img.ctypes.data, buf.ctypes.data, buf.size))
+        return buf.tobytes()
+
+
+def migrate(survey, params: dict | None = None, block: int = 50000, want_acc: bool = False):
+    """Image a synth.Survey in blocks of ``block`` traces (the reference's
+    ntblock).  Returns dict(image, fold, km?, pairs)."""
+    p = dict(survey.params)
+    if params:
+        p.update(params)
+    with Migration(p, survey.velocity) as m:
+        for b0 in range(0, survey.ntr, block):
+            m.add_traces(survey.headers[b0:b0 + block], survey.samples[b0:b0 + block])
+        image, fold = m.finish(want_fold=True)
+        out = dict(image=image, fold=fold, pairs=m.pairs())
+        if want_acc:
+            out["km"], out["fold_acc"] = m.accumulators()
+        return out

@@ -172,7 +172,7 @@ def line2d(n_cmp: int = 200, n_off: int = 48, ns: int = 1001, dt: float = 0.004,
     params = default_params(
         ns=ns, dt=float(np.float32(int(round(dt * 1e6)) / 1e6)),
         start_iline=start_il, end_iline=start_il + n_cmp, start_xline=4, end_xline=4,
-        iline_distance=d_cmp, xline_distance=d_cmp, nh=n_off, oh=-50.0 * u / 2.0 * 1.0,
+        iline_distance=d_cmp, xline_distance=d_cmp, nh=n_off, oh=0.0,
         dh=50.0 * u, aperture=aperture_m * u, anti_alias_cutoff=aa_cutoff)
     # oh = -dh/2 centres each class on its nominal offset: class k holds
     # offsets in [100k - 50, 100k + 50) units, so no offset sits on a class edge.
@@ -193,14 +193,18 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
             aa_cutoff: float = 100.0, seed: int = 2, mode: int = 1, output: int = 1,
             nh: int = 1, oh: float = 0.0, dh: float = 1.0e9, offsets=None,
             v_law=(1600.0, 500.0, 100.0, 8000.0), name: str = "patch3d",
-            trace_slice: slice | None = None) -> Survey:
+            trace_slice: slice | None = None, rotate_deg: float = 0.0,
+            origin=(0.0, 0.0)) -> Survey:
     """3-D patch: midpoints uniform over nx*bin x ny*bin metres, offsets
     U(0, max_offset) (or the given array), azimuths U(0, 2 pi); 30 Hz Ricker
     events from ``n_refl`` planar dipping reflectors (dips U(0, 30 deg),
     mirror-source traveltimes in a constant velocity per reflector) plus
     ``n_diff`` point diffractors (DSR traveltimes); smooth v_rms(x, t0) =
     v0 + vt*t0 + va*sin(2 pi x / lam).  Image nx x ny x ns at ``bin_m``.
-    ``trace_slice`` keeps only those traces (same seeded survey)."""
+    ``trace_slice`` keeps only those traces (same seeded survey).
+    ``rotate_deg``/``origin`` place the survey in world coordinates the way
+    the reference undoes it (Kirchhoff.c:1297-1304): grid (u, v) maps to
+    x = ox + cos(a) u - sin(a) v, y = oy + sin(a) u + cos(a) v."""
     rng = np.random.default_rng(seed)
     start = int(math.ceil(max_offset / 2.0 / bin_m)) + 4
     x0 = start * bin_m
@@ -227,7 +231,14 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
     sy = np.rint(mys - h * np.sin(az)).astype(np.int64)
     gx = np.rint(mxs + h * np.cos(az)).astype(np.int64)
     gy = np.rint(mys + h * np.sin(az)).astype(np.int64)
-    if min(sx.min(), sy.min(), gx.min(), gy.min()) < 0:
+    if rotate_deg != 0.0 or origin != (0.0, 0.0):
+        ca, sa = math.cos(math.radians(rotate_deg)), math.sin(math.radians(rotate_deg))
+        wx = lambda u, v: np.rint(origin[0] + ca * u - sa * v).astype(np.int64)
+        wy = lambda u, v: np.rint(origin[1] + sa * u + ca * v).astype(np.int64)
+        hsx, hsy, hgx, hgy = wx(sx, sy), wy(sx, sy), wx(gx, gy), wy(gx, gy)
+    else:
+        hsx, hsy, hgx, hgy = sx, sy, gx, gy
+    if min(hsx.min(), hsy.min(), hgx.min(), hgy.min()) < 0:
         raise ValueError("survey extends below coordinate 0")
     n = sx.size
     samples = np.zeros((n, ns), dtype=np.float64)
@@ -255,7 +266,7 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
                                                       (gy[:, None] - d_y[None, c0:c1]) ** 2) / dv[None, c0:c1] ** 2)
         _add_events(samples, ts + tg, np.broadcast_to(d_amp[c0:c1], (n, c1 - c0)).copy(), dt, freq, hw)
     samples = segy.ibm_roundtrip(samples.astype(np.float32))
-    hdr = segy.trace_headers(sx, sy, gx, gy, ns, int(round(dt * 1e6)))
+    hdr = segy.trace_headers(hsx, hsy, hgx, hgy, ns, int(round(dt * 1e6)))
     # velocity grid at the image inlines (v does not depend on y)
     t0 = np.arange(ns) * dt
     xs = (start + np.arange(nx)) * bin_m
@@ -266,6 +277,7 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
         ns=ns, dt=float(np.float32(int(round(dt * 1e6)) / 1e6)), start_iline=start,
         end_iline=start + nx, start_xline=start, end_xline=start + ny,
         iline_distance=bin_m, xline_distance=bin_m, nh=nh, oh=oh, dh=dh, aperture=aperture,
-        anti_alias_cutoff=aa_cutoff, mode=mode, output=output)
+        anti_alias_cutoff=aa_cutoff, mode=mode, output=output, ox=float(origin[0]),
+        oy=float(origin[1]), angle_e_to_n_deg=float(rotate_deg))
     info = dict(seed=seed, x0=x0, y0=y0)
     return Survey(name, params, vel, hdr, samples, info)

@@ -1,0 +1,80 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Each fixture is a small seeded survey imaged by the reference's own
+``kirchhoff()`` (Kirchhoff.c), compiled from the reference checkout with the
+documented flags by ``oracle/refbuild.py`` and run as independent ranks.
+Stored per fixture (``<name>.npz``):
+
+    params        JSON of the kpstm_params values
+    vel_*         the v_rms grid (kpstm_velocity fields) and values
+    headers       [ntr, 60] int32 trace-header words (host order)
+    ibm           [ntr, ns] uint32 IBM sample words (the exact file contents)
+    image         [nx_total, ny, nh, ns] float32: the SU files of all jobs,
+                  concatenated in job order (the reference's combine script)
+    su_headers    [ntraces, 60] int32: the SU header words it wrote
+    jobs          (jobs_x, jobs_y)
+
+Run here (needs the reference checkout and gcc):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import refbuild  # noqa: E402
+from random_gb300 import segy, synth  # noqa: E402
+
+HERE = Path(__file__).resolve().parent
+
+
+def fixtures():
+    """name -> (survey, jobs_x, jobs_y)"""
+    return {
+        # 2-D line, odd ns (the anti-alias mirror zeroes bins ns/2, ns/2+1),
+        # low-pass "off", one job
+        "g1_line_oddns": (synth.line2d(n_cmp=16, n_off=6, ns=251, seed=3), 1, 1),
+        # 2-D line, even ns, 40 Hz low-pass, image cut into 3 slabs
+        "g2_line_slabs": (synth.line2d(n_cmp=12, n_off=6, ns=300, seed=5, aa_cutoff=40.0), 3, 1),
+        # 3-D, rotated survey with a non-zero origin, 4 offset classes (some
+        # traces beyond the last class), slab cull active, 2 x 2 slabs
+        "g3_patch_rotated": (synth.patch3d(ntr=240, ns=161, dt=0.004, nx=8, ny=6, bin_m=25.0,
+                                           max_offset=1000.0, n_refl=2, n_diff=6, freq=25.0,
+                                           aperture=300.0, aa_cutoff=60.0, seed=7, mode=0,
+                                           output=0, nh=4, oh=0.0, dh=200.0, rotate_deg=30.0,
+                                           origin=(1000.0, 2000.0)), 2, 2),
+    }
+
+
+def run_reference(s, jx: int, jy: int, work: Path):
+    s.write_files(work / "data.segy", work / "vel.segy")
+    cfg = refbuild.RefConfig(**s.ref_config(jobs_x=jx, jobs_y=jy))
+    binary = refbuild.compile(cfg, tag="golden")
+    refbuild.run(binary, work / "run", work / "data.segy", work / "vel.segy", nprocs=jx * jy)
+    return refbuild.read_image(work / "run", s.ns, jx * jy)
+
+
+def main():
+    for name, (s, jx, jy) in fixtures().items():
+        with tempfile.TemporaryDirectory() as td:
+            hdr, img = run_reference(s, jx, jy, Path(td))
+        v = s.velocity
+        np.savez_compressed(
+            HERE / f"{name}.npz",
+            params=json.dumps(s.params), jobs=np.array([jx, jy]),
+            vel_grid=np.array([v.n_iline, v.n_xline, v.nsm, v.o_iline, v.o_xline, v.d_iline, v.d_xline]),
+            vel_dtm=np.float32(v.dtm), vel=v.vrms.astype(np.float32),
+            headers=s.headers, ibm=segy.ieee_to_ibm(s.samples), image=img.astype(np.float32),
+            su_headers=hdr.astype(np.int32))
+        print(name, s.ntr, "traces ->", img.shape)
+
+
+if __name__ == "__main__":
+    main()
