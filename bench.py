@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark: 3-D Kirchhoff PSTM, 1e6 traces x 1501 samples (2 ms) into a
+400 x 400 x 1501 stack image at 25 m bins, aperture 3000 m, triangle
+anti-alias, spreading + obliquity weights (KPSTM_MODE_FULL), fp32.
+
+A step is one block of 50,000 traces (the reference's ntblock,
+Kirchhoff.c:63) migrated into the whole image: kpstm_add_traces_device on
+inputs already in HBM (the survey is synthesised on the GPU once, 6 GB).
+Metric: Gsample-trace pairs/s, one pair = one (trace, in-aperture image
+column, output sample) = one pass of Kirchhoff.c:1374-1399.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank images its own slab of a wider survey (the
+reference's independent image slabs, Kirchhoff.c:280-300), so per-GPU work
+is fixed ("weak" scaling) and there is no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gsample-trace pairs/s"
+UNIT = "Gpairs/s"
+NS, DT = 1501, 0.002
+NX = NY = 400
+SURVEY_TRACES = 1_000_000
+STEP_TRACES = 50_000
+PEAKS = {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0)),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        if shutil.which("nvidia-smi") is None:
+            return
+        self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                   "--format=csv,noheader,nounits", "-lms", "200"],
+                                  stdout=self.f, stderr=subprocess.DEVNULL)
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax.append(float(c[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- workload
+def survey_model(rank: int = 0, ntr: int = SURVEY_TRACES):
+    from random_gb300 import synth
+    # each rank: its own 10 km x 10 km slab (x shifted), same statistics
+    return synth.patch3d_model(ntr, ns=NS, dt=DT, nx=NX, ny=NY, bin_m=25.0, max_offset=4000.0,
+                               n_refl=8, n_diff=200, freq=30.0, aperture=3000.0, aa_cutoff=100.0,
+                               seed=2 + rank, mode=1, output=1, x_shift=rank * 20000.0)
+
+
+def algorithmic_bytes_per_step(model, ntr_step: int, row_floats: int) -> int:
+    """Compulsory bytes of one imaging launch: the block's tap tables read
+    once, geometry, the image accumulators (sums + counts) read and written
+    once, and the velocity rows."""
+    ncol = NX * NY
+    return ntr_step * row_floats * 4 + ntr_step * 32 + ncol * NS * 4 * 2 * 2 + NX * NS * 8
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(n_traces: int, n_procs: int, opt: str = "-O3"):
+    """The reference's kirchhoff() on this host's cores: the image is cut
+    into 400 one-iline slabs (its own decomposition, Kirchhoff.c:280-300) and
+    n_procs of them, spread across the image, run as independent ranks over
+    the first n_traces traces of the same survey.  Returns (pairs, seconds)."""
+    from oracle import refbuild
+    from random_gb300 import synth
+    sm = synth.patch3d_model(SURVEY_TRACES, ns=NS, dt=DT, nx=NX, ny=NY, bin_m=25.0, max_offset=4000.0,
+                             n_refl=8, n_diff=200, freq=30.0, aperture=3000.0, aa_cutoff=100.0, seed=2,
+                             mode=1, output=1, trace_slice=slice(0, n_traces))
+    s = sm.survey
+    s.samples = synth.synthesize_numpy(sm)
+    jobs = sorted({int((k + 0.5) * NX / n_procs) for k in range(n_procs)})
+    work = Path(tempfile.mkdtemp(prefix="kref_"))
+    try:
+        s.write_files(work / "data.segy", work / "vel.segy")
+        cfg = refbuild.RefConfig(**s.ref_config(jobs_x=NX, jobs_y=1, ntblock=s.ntr))
+        binary = refbuild.compile(cfg, opt=opt, tag="bench")
+        (work / "run" / "image_dir").mkdir(parents=True, exist_ok=True)
+        for name in ("data.segy", "vel.segy"):
+            os.symlink(work / name, work / "run" / name)
+        t0 = time.perf_counter()
+        procs = [subprocess.Popen([str(binary)], cwd=work / "run", stdout=subprocess.DEVNULL,
+                                  stderr=subprocess.DEVNULL, stdin=subprocess.DEVNULL,
+                                  env=dict(os.environ, KPSTM_REF_RANK=str(j), KPSTM_REF_SIZE=str(NX)))
+                 for j in jobs]
+        for p in procs:
+            p.wait()
+        secs = time.perf_counter() - t0
+        if any(p.returncode for p in procs):
+            raise RuntimeError("reference rank failed")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    # pairs: in-aperture (trace, column) of the sampled slabs, float32 test as Kirchhoff.c:1351-1354
+    p = s.params
+    h = s.headers.astype(np.float64)
+    cx = (0.5 * (h[:, 18] + h[:, 20])).astype(np.float32)
+    cy = (0.5 * (h[:, 19] + h[:, 21])).astype(np.float32)
+    IY = ((p["start_xline"] + np.arange(NY)) * 25.0).astype(np.float32)
+    pairs = 0
+    for j in jobs:
+        IX = np.float32((p["start_iline"] + j) * 25.0)
+        dx = IX - cx
+        dy = IY[None, :] - cy[:, None]
+        d = np.sqrt(dx[:, None] * dx[:, None] + dy * dy)
+        pairs += int((d < np.float32(3000.0)).sum()) * NS
+    return pairs, secs, len(jobs)
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from random_gb300 import build, capi, segy, synth
+    from random_gb300.migration import Migration
+
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    peaks = load_peaks()
+    model = survey_model(rank)
+    s = model.survey
+    ntr = s.ntr
+    hdr_be = np.ascontiguousarray(segy.headers_be(s.headers))
+    d_hdr = torch.from_numpy(hdr_be).to(dev)
+    d_smp = synth.synthesize_torch(model, device=dev)
+    torch.cuda.synchronize()
+    block = args.traces_per_step
+    nblocks = ntr // block
+    row_bytes = NS * 4
+
+    m = Migration(s.params, s.velocity)
+    stream = torch.cuda.current_stream(dev)
+    m.set_stream(stream.cuda_stream)
+
+    def step(i):
+        b = i % nblocks
+        m.add_traces_device(d_hdr.data_ptr() + b * block * 240, d_smp.data_ptr() + b * block * row_bytes, block)
+
+    for i in range(args.warmup):
+        step(i)
+    m.synchronize()
+    m.profile(True)
+    m.profile_read()
+    pairs0 = m.pairs()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if world > 1:
+        dist.barrier()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    prof = m.profile_read()
+    m.profile(False)
+    pairs = m.pairs() - pairs0
+    tot = torch.tensor([elapsed, float(pairs)], dtype=torch.float64, device=dev)
+    if world > 1:
+        mx = tot[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm_ = tot[1:].clone()
+        dist.all_reduce(sm_, op=dist.ReduceOp.SUM)
+        elapsed_max, pairs_all = float(mx.item()), float(sm_.item())
+    else:
+        elapsed_max, pairs_all = elapsed, float(pairs)
+    value = pairs_all / elapsed_max / 1e9
+
+    # roofline of the imaging kernel (dominant: see profile shares)
+    launches = max(1, int(prof["image_launches"]))
+    t_launch = prof["image_ms"] / 1e3 / launches
+    row_floats = 2 * (NS + 2 * m.dims["trange_max"] - 3)
+    row_floats = (row_floats + 3) & ~3
+    b_alg = algorithmic_bytes_per_step(model, block, row_floats)
+    achieved = b_alg / t_launch / 1e9
+    pairs_per_launch = pairs / launches
+    roofline = {
+        "bound": "hbm", "achieved": round(achieved, 3), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": round(achieved / peaks["hbm_gbs"], 6), "traffic": None,
+        "peak_source": peaks["source"], "kernel": "k_image (full mode)",
+        "algorithmic_bytes_per_launch": b_alg, "launch_ms": round(t_launch * 1e3, 3),
+        "pairs_per_launch": pairs_per_launch,
+        "binding": "issue slots (no tensor work; HBM bytes per pair are ~1e-3): see profiles/",
+        "image_kernel_share": round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4),
+    }
+    del m
+
+    # -------- e2e through the C ABI from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        nb = min(nblocks, 4)
+        h_hdr = torch.from_numpy(hdr_be[:nb * block]).pin_memory()
+        h_smp = d_smp[:nb * block].cpu().pin_memory()
+        m2 = Migration(s.params, s.velocity)
+        out = torch.empty((NX, NY, 1, NS), dtype=torch.float32).pin_memory()
+        # one untimed block to create the staging buffers
+        m2.add_traces_ptr(h_hdr.data_ptr(), h_smp.data_ptr(), block)
+        m2.synchronize()
+        m2.reset()
+        pe0 = m2.pairs()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            b = i % nb
+            m2.add_traces_ptr(h_hdr.data_ptr() + b * block * 240, h_smp.data_ptr() + b * block * row_bytes, block)
+        m2.finish_ptr(out.data_ptr())
+        t_e2e = time.perf_counter() - t0
+        pe = m2.pairs() - pe0
+        del m2
+        e2e = {"value": round(pe / t_e2e / 1e9, 4), "unit": UNIT,
+               "h2d_bytes_per_step": block * (240 + row_bytes),
+               "d2h_bytes_per_step": int(out.numel() * 4 / args.steps) + 4,
+               "note": "kpstm_add_traces from pinned host buffers every step; one kpstm_finish "
+                       "(image to host) closes the timed region; wall clock"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cores = host_cores()
+        pairs_c, secs_c, nslab = cpu_sample(args.cpu_traces, cores)
+        cpu = {"value": round(pairs_c / secs_c / 1e9, 4), "unit": UNIT, "cores": nslab, "kind": "reference",
+               "sample": f"reference kirchhoff() (-O3 -ffast-math, MPI/FFTW stand-ins) on {nslab} of its "
+                         f"400 one-iline slabs, first {args.cpu_traces} traces of the survey, one rank per "
+                         f"core: {pairs_c} pairs in {secs_c:.2f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(elapsed_max / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 3-D survey: 8 dipping reflectors + 200 diffractors, 30 Hz Ricker)",
+            "config": {"workload": "3-D PSTM, 1e6 traces x 1501 samples @ 2 ms, 400x400x1501 stack image at "
+                                   "25 m, aperture 3000 m, triangle anti-alias + spreading/obliquity, fp32",
+                       "traces_per_step": block, "survey_traces": ntr, "mode": "full",
+                       "l2": "inputs larger than L2: 613 MB tap tables + 1.9 GB image accumulators per step",
+                       "parallelism": f"image slabs x{world}"},
+            "gpu_launches": int(prof["image_launches"] + prof["other_launches"]),
+            "pairs": int(pairs_all), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "profile_ms": {"image": round(prof["image_ms"], 3), "prep": round(prof["prep_ms"], 3)},
+        }
+        print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = host_cores()
+    vals, pairs_t, secs_t = [], 0, 0.0
+    for i in range(args.warmup + args.steps):
+        pairs, secs, nslab = cpu_sample(args.ref_traces, cores)
+        if i >= args.warmup:
+            vals.append(pairs / secs / 1e9)
+            pairs_t += pairs
+            secs_t += secs
+    value = pairs_t / secs_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs_t / args.steps * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (same seeded survey as the GPU arm)",
+        "config": {"workload": "3-D PSTM, 1e6 traces x 1501 samples @ 2 ms, 400x400x1501 stack image at "
+                               "25 m, aperture 3000 m (the reference's own operator: nearest-sample T, "
+                               "fixed triangle)", "sample_traces": args.ref_traces, "slabs": nslab},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nslab, "kind": "reference",
+                         "sample": f"{nslab} of 400 one-iline slabs x first {args.ref_traces} traces per step"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--traces-per-step", type=int, default=STEP_TRACES)
+    ap.add_argument("--cpu-traces", type=int, default=3000)
+    ap.add_argument("--ref-traces", type=int, default=1500)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

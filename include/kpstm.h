@@ -180,6 +180,26 @@ int kpstm_pair_count(const kpstm_ctx *ctx, int64_t *pairs);
 /* Device synchronisation of the context's stream. */
 int kpstm_synchronize(kpstm_ctx *ctx);
 
+/* Run the context's device work on the caller's CUDA stream (a
+   cudaStream_t; NULL restores the context's own stream), so that a host
+   framework can order its own work and timers with it.  No counterpart in
+   the reference, which has no device. */
+int kpstm_set_stream(kpstm_ctx *ctx, void *cuda_stream);
+
+/* Per-stage device timing with CUDA events on the compute stream (no
+   counterpart in the reference, which only prints wall clocks,
+   Kirchhoff.c:243, 338, 362).  While enabled every stage launch is
+   bracketed by events; kpstm_profile_read synchronises, sums and resets. */
+typedef struct {
+    int64_t image_launches;   /* imaging kernel launches */
+    double image_ms;          /* summed imaging kernel time */
+    double prep_ms;           /* geometry + bucketing + integral prep */
+    double finish_ms;         /* finishing kernels */
+    int64_t other_launches;   /* all other kernel launches */
+} kpstm_profile;
+int kpstm_profile_enable(kpstm_ctx *ctx, int enable);
+int kpstm_profile_read(kpstm_ctx *ctx, kpstm_profile *out);
+
 /* ---- stand-alone set-up helpers (host only) -------------------------------- */
 
 /* create_aliasfilter, Kirchhoff.c:380-441: trangeMax and the low-pass

@@ -54,6 +54,11 @@ class KpstmVelocity(C.Structure):
     ]
 
 
+class KpstmProfile(C.Structure):
+    _fields_ = [("image_launches", C.c_int64), ("image_ms", C.c_double), ("prep_ms", C.c_double),
+                ("finish_ms", C.c_double), ("other_launches", C.c_int64)]
+
+
 class KpstmDims(C.Structure):
     _fields_ = [
         ("Nx", C.c_int32), ("Ny", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
@@ -132,6 +137,9 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_get_accumulators", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_pair_count", C.c_int, [_VOIDP, C.POINTER(i64)])
     _sig(lib, "kpstm_synchronize", C.c_int, [_VOIDP])
+    _sig(lib, "kpstm_set_stream", C.c_int, [_VOIDP, _VOIDP])
+    _sig(lib, "kpstm_profile_enable", C.c_int, [_VOIDP, C.c_int])
+    _sig(lib, "kpstm_profile_read", C.c_int, [_VOIDP, C.POINTER(KpstmProfile)])
     _sig(lib, "kpstm_aliasfilter", C.c_int, [i32, C.c_float, C.c_double, C.c_double, C.c_double,
                                             C.POINTER(i32), _VOIDP])
     _sig(lib, "kpstm_ibm_to_ieee", C.c_int, [_VOIDP, _VOIDP, i64])

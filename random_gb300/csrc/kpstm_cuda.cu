@@ -64,7 +64,50 @@ struct kpstm_ctx {
     unsigned long long *d_hits;
     /* finishing scratch */
     float *d_x, *d_y;
+    /* stream handling / profiling */
+    cudaStream_t own_cs;
+    int prof;
+    int nev, capev;
+    cudaEvent_t *ev;             /* pairs: start, stop */
+    int *evstage;                /* 0 image, 1 prep, 2 finish */
+    int *evlaunches;
 };
+
+/* Stage bracketing for kpstm_profile_*; no-ops when profiling is off. */
+static int prof_begin(kpstm_ctx *c)
+{
+    if (!c->prof) return -1;
+    if (c->nev + 2 > c->capev) {
+        int cap = c->capev ? 2 * c->capev : 256;
+        cudaEvent_t *ev = (cudaEvent_t *)realloc(c->ev, sizeof(cudaEvent_t) * cap);
+        if (!ev) return -1;
+        c->ev = ev;
+        int *st = (int *)realloc(c->evstage, sizeof(int) * cap);
+        if (!st) return -1;
+        c->evstage = st;
+        int *nl = (int *)realloc(c->evlaunches, sizeof(int) * cap);
+        if (!nl) return -1;
+        c->evlaunches = nl;
+        c->capev = cap;
+    }
+    int i = c->nev;
+    if (cudaEventCreate(&c->ev[i]) != cudaSuccess) return -1;
+    if (cudaEventCreate(&c->ev[i + 1]) != cudaSuccess) {
+        cudaEventDestroy(c->ev[i]);
+        return -1;
+    }
+    cudaEventRecord(c->ev[i], c->cs);
+    c->nev += 2;
+    return i;
+}
+
+static void prof_end(kpstm_ctx *c, int i, int stage, int launches)
+{
+    if (i < 0) return;
+    cudaEventRecord(c->ev[i + 1], c->cs);
+    c->evstage[i] = stage;
+    c->evlaunches[i] = launches;
+}
 
 static int kp_free_all(kpstm_ctx *c);
 
@@ -177,6 +220,7 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     g.IYc = s->IYc;
     g.nh = p->nh;
     g.stack = p->output == KPSTM_OUT_STACK;
+    int pe = prof_begin(c);
     k_geometry<<<(unsigned)((ntr + 255) / 256), 256, 0, c->cs>>>(g);
     KP_CUDA(cudaGetLastError());
 
@@ -201,6 +245,7 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     pa.dt = p->dt;
     k_prep<<<(unsigned)((ntr + 127) / 128), 128, 0, c->cs>>>(pa);
     KP_CUDA(cudaGetLastError());
+    prof_end(c, pe, 1, 3);
 
     KpImageArgs a;
     memset(&a, 0, sizeof(a));
@@ -233,7 +278,9 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     a.tile_r2 = r * r;
     a.aax = (float)(p->iline_distance / p->dt);
     a.aay = (float)(p->xline_distance / p->dt);
+    int pi = prof_begin(c);
     KP_CUDA(launch_image(c, a));
+    prof_end(c, pi, 0, 1);
     return KPSTM_OK;
 }
 
@@ -345,6 +392,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     if (!st) {
         do {
             cudaError_t e = cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking);
+            c->own_cs = c->cs;
             if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xs, cudaStreamNonBlocking);
             for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
                 e = cudaEventCreateWithFlags(&c->copy_done[k], cudaEventDisableTiming);
@@ -421,6 +469,7 @@ static int kp_free_all(kpstm_ctx *c)
 {
     if (!c) return KPSTM_OK;
     if (c->cs) cudaStreamSynchronize(c->cs);
+    if (c->own_cs && c->own_cs != c->cs) cudaStreamSynchronize(c->own_cs);
     if (c->xs) cudaStreamSynchronize(c->xs);
     void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_c4, c->d_c4r,
                     c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
@@ -432,7 +481,11 @@ static int kp_free_all(kpstm_ctx *c)
         if (c->copy_done[k]) cudaEventDestroy(c->copy_done[k]);
         if (c->comp_done[k]) cudaEventDestroy(c->comp_done[k]);
     }
-    if (c->cs) cudaStreamDestroy(c->cs);
+    for (int i = 0; i < c->nev; ++i) cudaEventDestroy(c->ev[i]);
+    free(c->ev);
+    free(c->evstage);
+    free(c->evlaunches);
+    if (c->own_cs) cudaStreamDestroy(c->own_cs);
     if (c->xs) cudaStreamDestroy(c->xs);
     free(c);
     return KPSTM_OK;
@@ -556,6 +609,7 @@ static int finish_dev(kpstm_ctx *c, float *out, float *fold)
     if (out) {
         int st = ensure_finish_scratch(c);
         if (st) return st;
+        int pf = prof_begin(c);
         k_deriv<<<1024, 256, 0, c->cs>>>(c->d_km, c->d_cnt, ncol, ncls, ns, c->p.dt, c->d_x);
         KP_CUDA(cudaGetLastError());
         size_t smem = sizeof(float) * (((2 * (size_t)ns + 3) & ~size_t(3)) + (size_t)ns * KP_LP_ROWS);
@@ -564,6 +618,7 @@ static int finish_dev(kpstm_ctx *c, float *out, float *fold)
         k_lowpass<<<(unsigned)((nrows + KP_LP_ROWS - 1) / KP_LP_ROWS), 256, smem, c->cs>>>(c->d_x, c->d_h, nrows,
                                                                                           ns, out);
         KP_CUDA(cudaGetLastError());
+        prof_end(c, pf, 2, 2);
     }
     if (fold) {
         k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, ncol, ncls, ns, fold);
@@ -657,5 +712,50 @@ extern "C" int kpstm_write_su(const kpstm_ctx *c, const float *image, void *dst,
             }
         }
     }
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_set_stream(kpstm_ctx *c, void *stream)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    cudaStream_t next = stream ? (cudaStream_t)stream : c->own_cs;
+    if (next == c->cs) return KPSTM_OK;
+    /* order the new stream after everything queued so far */
+    cudaEvent_t e;
+    KP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    KP_CUDA(cudaEventRecord(e, c->cs));
+    KP_CUDA(cudaStreamWaitEvent(next, e, 0));
+    cudaEventDestroy(e);
+    c->cs = next;
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_profile_enable(kpstm_ctx *c, int enable)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    c->prof = enable ? 1 : 0;
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_profile_read(kpstm_ctx *c, kpstm_profile *out)
+{
+    if (!c || !out) return KPSTM_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    for (int i = 0; i + 1 < c->nev; i += 2) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]) != cudaSuccess) ms = 0.0f;
+        if (c->evstage[i] == 0) {
+            out->image_ms += ms;
+            out->image_launches += c->evlaunches[i];
+        } else {
+            if (c->evstage[i] == 1) out->prep_ms += ms;
+            else out->finish_ms += ms;
+            out->other_launches += c->evlaunches[i];
+        }
+        cudaEventDestroy(c->ev[i]);
+        cudaEventDestroy(c->ev[i + 1]);
+    }
+    c->nev = 0;
     return KPSTM_OK;
 }

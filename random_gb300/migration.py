@@ -101,6 +101,17 @@ class Migration:
         capi.check("kpstm_pair_count", self._lib.kpstm_pair_count(self._h, C.byref(v)))
         return v.value
 
+    def set_stream(self, stream_handle: int | None) -> None:
+        capi.check("kpstm_set_stream", self._lib.kpstm_set_stream(self._h, stream_handle))
+
+    def profile(self, enable: bool = True) -> None:
+        capi.check("kpstm_profile_enable", self._lib.kpstm_profile_enable(self._h, int(enable)))
+
+    def profile_read(self) -> dict:
+        pr = capi.KpstmProfile()
+        capi.check("kpstm_profile_read", self._lib.kpstm_profile_read(self._h, C.byref(pr)))
+        return {f: getattr(pr, f) for f, _ in capi.KpstmProfile._fields_}
+
     def synchronize(self) -> None:
         capi.check("kpstm_synchronize", self._lib.kpstm_synchronize(self._h))
 

@@ -187,14 +187,26 @@ def vrms_3d(x: np.ndarray, t0: np.ndarray, v0: float, vt: float, va: float,
     return v0 + vt * t0 + va * np.sin(2.0 * math.pi * x / lam)
 
 
-def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int = 400,
-            bin_m: float = 25.0, max_offset: float = 4000.0, n_refl: int = 8,
-            n_diff: int = 200, freq: float = 30.0, aperture: float = 3000.0,
-            aa_cutoff: float = 100.0, seed: int = 2, mode: int = 1, output: int = 1,
-            nh: int = 1, oh: float = 0.0, dh: float = 1.0e9, offsets=None,
-            v_law=(1600.0, 500.0, 100.0, 8000.0), name: str = "patch3d",
-            trace_slice: slice | None = None, rotate_deg: float = 0.0,
-            origin=(0.0, 0.0)) -> Survey:
+@dataclass
+class Patch3DModel:
+    """Geometry, events and v_rms of a 3-D patch survey; samples are
+    synthesised separately (numpy here, torch on a GPU for full-size runs)."""
+    survey: Survey                       # headers/params/velocity; samples empty
+    coords: np.ndarray                   # [ntr, 4] float64 grid-frame sx, sy, gx, gy
+    refl: dict                           # t0, vk, z0, nrm [n, 3], amp, xc, yc
+    diff: dict                           # x, y, t0, v, amp
+    freq: float
+    half_width: int
+
+
+def patch3d_model(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int = 400,
+                  bin_m: float = 25.0, max_offset: float = 4000.0, n_refl: int = 8,
+                  n_diff: int = 200, freq: float = 30.0, aperture: float = 3000.0,
+                  aa_cutoff: float = 100.0, seed: int = 2, mode: int = 1, output: int = 1,
+                  nh: int = 1, oh: float = 0.0, dh: float = 1.0e9, offsets=None,
+                  v_law=(1600.0, 500.0, 100.0, 8000.0), name: str = "patch3d",
+                  trace_slice: slice | None = None, rotate_deg: float = 0.0,
+                  origin=(0.0, 0.0), x_shift: float = 0.0) -> Patch3DModel:
     """3-D patch: midpoints uniform over nx*bin x ny*bin metres, offsets
     U(0, max_offset) (or the given array), azimuths U(0, 2 pi); 30 Hz Ricker
     events from ``n_refl`` planar dipping reflectors (dips U(0, 30 deg),
@@ -204,18 +216,21 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
     ``trace_slice`` keeps only those traces (same seeded survey).
     ``rotate_deg``/``origin`` place the survey in world coordinates the way
     the reference undoes it (Kirchhoff.c:1297-1304): grid (u, v) maps to
-    x = ox + cos(a) u - sin(a) v, y = oy + sin(a) u + cos(a) v."""
+    x = ox + cos(a) u - sin(a) v, y = oy + sin(a) u + cos(a) v.
+    ``x_shift`` moves the whole survey and image along x (one slab per
+    rank in multi-GPU runs)."""
     rng = np.random.default_rng(seed)
     start = int(math.ceil(max_offset / 2.0 / bin_m)) + 4
+    start += int(round(x_shift / bin_m))
     x0 = start * bin_m
-    y0 = start * bin_m
+    y0 = (int(math.ceil(max_offset / 2.0 / bin_m)) + 4) * bin_m
+    start_y = int(round(y0 / bin_m))
     W, H = nx * bin_m, ny * bin_m
     mxs = rng.uniform(x0, x0 + W, ntr)
     mys = rng.uniform(y0, y0 + H, ntr)
     off = rng.uniform(0.0, max_offset, ntr) if offsets is None else np.asarray(offsets, float)
     az = rng.uniform(0.0, 2.0 * math.pi, ntr)
     v0, vt, va, lam = v_law
-    # events (drawn before slicing so every slice sees the same model)
     r_t0 = rng.uniform(0.4, 0.8 * (ns - 1) * dt, n_refl)
     r_dip = np.radians(rng.uniform(0.0, 30.0, n_refl))
     r_az = rng.uniform(0.0, 2.0 * math.pi, n_refl)
@@ -240,44 +255,88 @@ def patch3d(ntr: int, ns: int = 1501, dt: float = 0.002, nx: int = 400, ny: int 
         hsx, hsy, hgx, hgy = sx, sy, gx, gy
     if min(hsx.min(), hsy.min(), hgx.min(), hgy.min()) < 0:
         raise ValueError("survey extends below coordinate 0")
-    n = sx.size
-    samples = np.zeros((n, ns), dtype=np.float64)
-    hw = int(math.ceil(0.06 / dt))
     xc, yc = x0 + 0.5 * W, y0 + 0.5 * H
-    # planar reflectors: plane through (xc, yc, z0) with unit normal nrm
-    for k in range(n_refl):
-        vk = v0 + vt * r_t0[k]
-        z0 = 0.5 * vk * r_t0[k]
-        nrm = np.array([math.sin(r_dip[k]) * math.cos(r_az[k]),
-                        math.sin(r_dip[k]) * math.sin(r_az[k]), math.cos(r_dip[k])])
-        dist_s = nrm[2] * z0 - (nrm[0] * (sx - xc) + nrm[1] * (sy - yc))
-        mx_ = sx + 2.0 * dist_s * nrm[0]
-        my_ = sy + 2.0 * dist_s * nrm[1]
-        mz_ = 2.0 * dist_s * nrm[2]
-        te = np.sqrt((mx_ - gx) ** 2 + (my_ - gy) ** 2 + mz_ ** 2) / vk
-        _add_events(samples, te[:, None], np.full((n, 1), r_amp[k]), dt, freq, hw)
-    # diffractors (chunks bound memory)
-    dv = vrms_3d(d_x, d_t0, v0, vt, va, lam)
-    for c0 in range(0, n_diff, 32):
-        c1 = min(n_diff, c0 + 32)
-        ts = np.sqrt(0.25 * d_t0[None, c0:c1] ** 2 + ((sx[:, None] - d_x[None, c0:c1]) ** 2 +
-                                                      (sy[:, None] - d_y[None, c0:c1]) ** 2) / dv[None, c0:c1] ** 2)
-        tg = np.sqrt(0.25 * d_t0[None, c0:c1] ** 2 + ((gx[:, None] - d_x[None, c0:c1]) ** 2 +
-                                                      (gy[:, None] - d_y[None, c0:c1]) ** 2) / dv[None, c0:c1] ** 2)
-        _add_events(samples, ts + tg, np.broadcast_to(d_amp[c0:c1], (n, c1 - c0)).copy(), dt, freq, hw)
-    samples = segy.ibm_roundtrip(samples.astype(np.float32))
+    vk = v0 + vt * r_t0
+    nrm = np.stack([np.sin(r_dip) * np.cos(r_az), np.sin(r_dip) * np.sin(r_az), np.cos(r_dip)], 1)
+    refl = dict(t0=r_t0, vk=vk, z0=0.5 * vk * r_t0, nrm=nrm, amp=r_amp, xc=xc, yc=yc)
+    diff = dict(x=d_x, y=d_y, t0=d_t0, v=vrms_3d(d_x, d_t0, v0, vt, va, lam), amp=d_amp)
     hdr = segy.trace_headers(hsx, hsy, hgx, hgy, ns, int(round(dt * 1e6)))
-    # velocity grid at the image inlines (v does not depend on y)
     t0 = np.arange(ns) * dt
     xs = (start + np.arange(nx)) * bin_m
     vg = vrms_3d(xs[:, None], t0[None, :], v0, vt, va, lam).astype(np.float32)
-    vel = Velocity(n_iline=nx, n_xline=1, nsm=ns, o_iline=start, o_xline=start, d_iline=1,
+    vel = Velocity(n_iline=nx, n_xline=1, nsm=ns, o_iline=start, o_xline=start_y, d_iline=1,
                    d_xline=1000000, dtm=dt, vrms=segy.ibm_roundtrip(vg[:, None, :].copy()))
     params = default_params(
         ns=ns, dt=float(np.float32(int(round(dt * 1e6)) / 1e6)), start_iline=start,
-        end_iline=start + nx, start_xline=start, end_xline=start + ny,
+        end_iline=start + nx, start_xline=start_y, end_xline=start_y + ny,
         iline_distance=bin_m, xline_distance=bin_m, nh=nh, oh=oh, dh=dh, aperture=aperture,
         anti_alias_cutoff=aa_cutoff, mode=mode, output=output, ox=float(origin[0]),
         oy=float(origin[1]), angle_e_to_n_deg=float(rotate_deg))
     info = dict(seed=seed, x0=x0, y0=y0)
-    return Survey(name, params, vel, hdr, samples, info)
+    sv = Survey(name, params, vel, hdr, np.zeros((0, ns), np.float32), info)
+    coords = np.stack([sx, sy, gx, gy], 1).astype(np.float64)
+    return Patch3DModel(sv, coords, refl, diff, freq, int(math.ceil(0.06 / dt)))
+
+
+def _event_times(xp, c, refl, diff):
+    """Traveltimes [ntr, n_events] of all events for grid coords c [ntr, 4]
+    (xp = numpy or torch)."""
+    sx, sy, gx, gy = c[:, 0], c[:, 1], c[:, 2], c[:, 3]
+    cols = []
+    for k in range(len(refl["t0"])):
+        n0, n1, n2 = (float(v) for v in refl["nrm"][k])
+        dist_s = n2 * float(refl["z0"][k]) - (n0 * (sx - refl["xc"]) + n1 * (sy - refl["yc"]))
+        mx_ = sx + 2.0 * dist_s * n0
+        my_ = sy + 2.0 * dist_s * n1
+        mz_ = 2.0 * dist_s * n2
+        cols.append(xp.sqrt((mx_ - gx) ** 2 + (my_ - gy) ** 2 + mz_ ** 2) / float(refl["vk"][k]))
+    for k in range(len(diff["t0"])):
+        th = 0.25 * float(diff["t0"][k]) ** 2
+        v2 = float(diff["v"][k]) ** 2
+        ts = xp.sqrt(th + ((sx - float(diff["x"][k])) ** 2 + (sy - float(diff["y"][k])) ** 2) / v2)
+        tg = xp.sqrt(th + ((gx - float(diff["x"][k])) ** 2 + (gy - float(diff["y"][k])) ** 2) / v2)
+        cols.append(ts + tg)
+    return cols
+
+
+def synthesize_numpy(m: Patch3DModel) -> np.ndarray:
+    s = m.survey
+    ns, dt = s.ns, float(s.params["dt"])
+    n = m.coords.shape[0]
+    out = np.zeros((n, ns), np.float64)
+    amps = list(m.refl["amp"]) + list(m.diff["amp"])
+    for e, te in enumerate(_event_times(np, m.coords, m.refl, m.diff)):
+        _add_events(out, te[:, None], np.full((n, 1), float(amps[e])), dt, m.freq, m.half_width)
+    return segy.ibm_roundtrip(out.astype(np.float32))
+
+
+def synthesize_torch(m: Patch3DModel, device="cuda", chunk: int = 250_000):
+    """Same events as synthesize_numpy, computed on a GPU with torch (no IBM
+    round trip); returns a float32 tensor [ntr, ns] on ``device``."""
+    import torch
+    s = m.survey
+    ns, dt = s.ns, float(s.params["dt"])
+    n = m.coords.shape[0]
+    out = torch.zeros((n, ns), dtype=torch.float32, device=device)
+    amps = list(m.refl["amp"]) + list(m.diff["amp"])
+    k = torch.arange(-m.half_width, m.half_width + 1, device=device, dtype=torch.int64)
+    for c0 in range(0, n, chunk):
+        c1 = min(n, c0 + chunk)
+        c = torch.from_numpy(m.coords[c0:c1]).to(device)
+        rows = torch.arange(c1 - c0, device=device, dtype=torch.int64)[:, None] * ns
+        flat = out[c0:c1].view(-1)
+        for e, te in enumerate(_event_times(torch, c, m.refl, m.diff)):
+            idx = torch.floor(te / dt).to(torch.int64)[:, None] + k[None, :]
+            ok = (idx >= 0) & (idx < ns)
+            a = (math.pi * m.freq * (idx.to(torch.float64) * dt - te[:, None])) ** 2
+            w = ((1.0 - 2.0 * a) * torch.exp(-a) * float(amps[e])).to(torch.float32)
+            flat.index_add_(0, (rows + idx)[ok], w[ok])
+    return out
+
+
+def patch3d(ntr: int, **kw) -> Survey:
+    """A 3-D patch survey with numpy-synthesised samples (see patch3d_model)."""
+    m = patch3d_model(ntr, **kw)
+    s = m.survey
+    s.samples = synthesize_numpy(m)
+    return s

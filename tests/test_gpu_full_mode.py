@@ -1,0 +1,67 @@
+"""GPU full-physics mode (linear trace interpolation, obliquity/spreading
+weight, variable-width triangle anti-alias; no reference counterpart)
+against the FP64 CPU oracle restatement of the same operator.
+
+The GPU computes in fp32 with the SFU reciprocal square root, so results
+are not bit-identical; the bars below are the measured fp32-vs-fp64 error
+with margin: relative L2 of the accumulators <= 1e-4, fold counts equal
+except where the fp32 and fp64 traveltimes straddle the last sample."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from fixtures import rel_l2
+from random_gb300 import capi, synth
+from random_gb300.migration import migrate
+
+pytestmark = pytest.mark.gpu
+ACC_TOL = 1e-4
+
+
+def _survey(**kw):
+    base = dict(ntr=400, ns=301, dt=0.004, nx=10, ny=8, bin_m=25.0, max_offset=1200.0, n_refl=3,
+                n_diff=10, freq=25.0, aperture=500.0, aa_cutoff=60.0, seed=21, mode=capi.MODE_FULL,
+                output=capi.OUT_OFFSET_GATHERS, nh=3, oh=0.0, dh=400.0)
+    base.update(kw)
+    return synth.patch3d(**base)
+
+
+def _check(g, o):
+    assert rel_l2(g["km"], o["km"]) <= ACC_TOL, rel_l2(g["km"], o["km"])
+    mism = np.mean(g["fold"] != o["fold"])
+    assert mism <= 1e-4, mism
+    assert g["pairs"] == o["pairs"]
+
+
+@pytest.mark.parametrize("output", [capi.OUT_OFFSET_GATHERS, capi.OUT_STACK])
+def test_full_mode_matches_fp64_oracle(kpstm_lib, oracle_lib, output):
+    s = _survey(output=output)
+    g = migrate(s, want_acc=True)
+    o = oracle_lib.kirchhoff(s)
+    _check(g, o)
+    assert rel_l2(g["image"], o["image"]) <= ACC_TOL
+
+
+def test_full_mode_two_time_windows(kpstm_lib, oracle_lib):
+    """ns = 1501 (2 ms) is imaged in two register windows of 768 samples."""
+    s = _survey(ntr=150, ns=1501, dt=0.002, nx=4, ny=4, aperture=400.0, max_offset=800.0, nh=1, dh=1e9,
+                output=capi.OUT_STACK)
+    g = migrate(s, want_acc=True)
+    o = oracle_lib.kirchhoff(s)
+    _check(g, o)
+
+
+def test_full_mode_line(kpstm_lib, oracle_lib):
+    s = synth.line2d(n_cmp=40, n_off=8, ns=401, seed=13)
+    p = dict(mode=capi.MODE_FULL)
+    g = migrate(s, p, want_acc=True)
+    o = oracle_lib.kirchhoff(s, p)
+    _check(g, o)
+
+
+def test_full_mode_block_split_is_invisible(kpstm_lib):
+    s = _survey()
+    a = migrate(s, block=100_000, want_acc=True)
+    b = migrate(s, block=77, want_acc=True)
+    assert np.array_equal(a["km"], b["km"]) and np.array_equal(a["fold"], b["fold"])
