@@ -186,7 +186,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     peaks = load_peaks()
-    model = survey_model(rank)
+    model = survey_model(rank, args.survey_traces)
     s = model.survey
     ntr = s.ntr
     hdr_be = np.ascontiguousarray(segy.headers_be(s.headers))
@@ -198,7 +198,8 @@ def run_ours(args, rank, world, local_rank):
     row_bytes = NS * 4
 
     m = Migration(s.params, s.velocity)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream shared by the library and the timers
+    stream = torch.cuda.Stream(device=dev)
     m.set_stream(stream.cuda_stream)
 
     def step(i):
@@ -222,6 +223,7 @@ def run_ours(args, rank, world, local_rank):
         step(args.warmup + i)
     e1.record(stream)
     torch.cuda.synchronize()
+    m.synchronize()
     clk = clocks.stop()
     if world > 1:
         dist.barrier()
@@ -349,6 +351,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--traces-per-step", type=int, default=STEP_TRACES)
+    ap.add_argument("--survey-traces", type=int, default=SURVEY_TRACES,
+                    help="traces synthesised on the device (smaller only for profiling captures)")
     ap.add_argument("--cpu-traces", type=int, default=3000)
     ap.add_argument("--ref-traces", type=int, default=1500)
     ap.add_argument("--no-e2e", action="store_true")
