@@ -56,8 +56,9 @@ typedef enum {
     KPSTM_ERR_NO_DEVICE = 9,       /* no CUDA device visible */
     KPSTM_ERR_SEGY = 10,           /* malformed SEG-Y buffer */
     KPSTM_ERR_UNSUPPORTED = 11,    /* valid request this build does not implement */
-    KPSTM_ERR_TRANGE = 12          /* trangeMax < 2: the reference's triangle taps
+    KPSTM_ERR_TRANGE = 12,         /* trangeMax < 2: the reference's triangle taps
                                       (Kirchhoff.c:1391-1392) would read before the trace */
+    KPSTM_ERR_TOO_LARGE = 13       /* request exceeds the fixed scratch of kpstm_finish_noalloc */
 } kpstm_status;
 
 /* Imaging operator. */
@@ -199,6 +200,37 @@ typedef struct {
 } kpstm_profile;
 int kpstm_profile_enable(kpstm_ctx *ctx, int enable);
 int kpstm_profile_read(kpstm_ctx *ctx, kpstm_profile *out);
+
+/* ---- finishing without device allocation ------------------------------------ */
+
+/* Largest image (nx*ny*nh*ns samples) kpstm_finish_noalloc accepts. */
+#define KPSTM_NOALLOC_MAX_SAMPLES 4194304
+
+/* The finishing step of kpstm_finish for callers that must not allocate
+   device memory.  No counterpart in the reference (it has no device).
+
+   Some callers cannot call cudaMalloc: a process whose framework allocator
+   has already reserved the device memory it is allowed to use, or a
+   pipelined service that must not let cudaMalloc/cudaFree synchronise the
+   device between jobs.  This entry point allocates nothing: the caller
+   passes the accumulators and the output, all in device memory and in the
+   layout kpstm_get_accumulators returns ([nx][ny][nh][ns]; fold as floats,
+   1 + contributing traces), and the intermediate derivative traces and the
+   low-pass impulse response live in one fixed array compiled into the
+   library - about 17 MB that every GPU which loads the library holds until
+   the process exits.  Images larger than KPSTM_NOALLOC_MAX_SAMPLES samples
+   are refused with KPSTM_ERR_TOO_LARGE; params are checked as in
+   kpstm_create (no context is needed).
+
+   The first call on a device looks up that array's device address (with
+   the device current); make that first call before any stream capture.
+   Work is queued on cuda_stream (NULL: the default stream) and the call
+   returns without waiting; synchronise before reading d_out.  All calls on
+   a device share the one array, so calls whose work overlaps on the GPU
+   (other streams, other host threads) race and must be serialised by the
+   caller. */
+int kpstm_finish_noalloc(const kpstm_params *params, const float *d_km, const float *d_fold,
+                         float *d_out, void *cuda_stream);
 
 /* ---- stand-alone set-up helpers (host only) -------------------------------- */
 

@@ -25,8 +25,9 @@ STATUS = {
     0: "KPSTM_OK", 1: "KPSTM_ERR_INVALID_ARG", 2: "KPSTM_ERR_CUDA", 3: "KPSTM_ERR_OUT_OF_MEMORY",
     4: "KPSTM_ERR_VELOCITY_ZERO", 5: "KPSTM_ERR_VELOCITY_RANGE", 6: "KPSTM_ERR_GEOMETRY",
     7: "KPSTM_ERR_STATE", 8: "KPSTM_ERR_TIMEOUT", 9: "KPSTM_ERR_NO_DEVICE", 10: "KPSTM_ERR_SEGY",
-    11: "KPSTM_ERR_UNSUPPORTED", 12: "KPSTM_ERR_TRANGE",
+    11: "KPSTM_ERR_UNSUPPORTED", 12: "KPSTM_ERR_TRANGE", 13: "KPSTM_ERR_TOO_LARGE",
 }
+NOALLOC_MAX_SAMPLES = 4194304
 
 
 class KpstmParams(C.Structure):
@@ -140,6 +141,7 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_set_stream", C.c_int, [_VOIDP, _VOIDP])
     _sig(lib, "kpstm_profile_enable", C.c_int, [_VOIDP, C.c_int])
     _sig(lib, "kpstm_profile_read", C.c_int, [_VOIDP, C.POINTER(KpstmProfile)])
+    _sig(lib, "kpstm_finish_noalloc", C.c_int, [C.POINTER(KpstmParams), _VOIDP, _VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_aliasfilter", C.c_int, [i32, C.c_float, C.c_double, C.c_double, C.c_double,
                                             C.POINTER(i32), _VOIDP])
     _sig(lib, "kpstm_ibm_to_ieee", C.c_int, [_VOIDP, _VOIDP, i64])

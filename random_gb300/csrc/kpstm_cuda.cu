@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -757,5 +758,113 @@ extern "C" int kpstm_profile_read(kpstm_ctx *c, kpstm_profile *out)
         cudaEventDestroy(c->ev[i + 1]);
     }
     c->nev = 0;
+    return KPSTM_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Finishing without device allocation (kpstm_finish_noalloc).
+   The scratch a finishing pass needs - the derivative traces between
+   k_deriv and k_lowpass, and the low-pass impulse response - is this one
+   file-scope array instead of context buffers.  Nothing in it has to start
+   at zero: every call rewrites the parts it reads. */
+#define KP_NOALLOC_MAX_NS 32768
+static __device__ __align__(256) float g_noalloc_scratch[KPSTM_NOALLOC_MAX_SAMPLES + KP_NOALLOC_MAX_NS];
+
+/* Device address of g_noalloc_scratch per device, looked up once per device
+   with that device current (the array's name is only a host-side handle in
+   host code). */
+#define KP_NOALLOC_MAX_DEVICES 64
+static float *g_noalloc_ptr[KP_NOALLOC_MAX_DEVICES];
+static pthread_mutex_t g_noalloc_mu = PTHREAD_MUTEX_INITIALIZER;
+
+static int noalloc_scratch(float **out)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return KPSTM_ERR_NO_DEVICE;
+    if (dev < 0 || dev >= KP_NOALLOC_MAX_DEVICES) return KPSTM_ERR_UNSUPPORTED;
+    pthread_mutex_lock(&g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            pthread_mutex_unlock(&g_noalloc_mu);
+            return KPSTM_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = (float *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    pthread_mutex_unlock(&g_noalloc_mu);
+    return KPSTM_OK;
+}
+
+/* Low-pass impulse response h[m] = (1/ns) sum_k A[k] cos(2 pi k m / ns), with
+   the anti-alias spectrum A of Kirchhoff.c:380-441 evaluated per bin in the
+   same float/double steps as kpstm_aliasfilter (fs, den from the host). */
+__global__ void k_noalloc_impulse(int ns, float fs, float den, float *h)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= ns) return;
+    const int half = ns / 2;
+    double acc = 0.0;
+    for (int k = 0; k < ns; ++k) {
+        int j = k;
+        bool zero = (ns & 1) && (k == half || k == half + 1);
+        if (k > half) j = ns - k;
+        float a = 0.0f;
+        if (!zero) {
+            float x = __fmul_rn(__int2float_rn(j), fs);
+            float num = __fmul_rn(__fmul_rn(__fmul_rn(x, x), x), x);
+            a = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, (double)__fdiv_rn(num, den)))));
+        }
+        long long km = ((long long)k * m) % ns;
+        acc += (double)a * cos(6.283185307179586476925286766559 * (double)km / (double)ns);
+    }
+    h[m] = (float)(acc / ns);
+}
+
+/* k_deriv for accumulators in the caller's layout [col][cls][ns] with the
+   fold given as floats: x[t] = -dt*t*(km[t]-km[t-1])*dt/fold[t], x[0] = 0. */
+__global__ void k_deriv_caller(const float *km, const float *fold, int64_t n, int ns, float dt, float *x)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int t = (int)(i % ns);
+        float v = 0.0f;
+        if (t > 0)
+            v = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(-dt, __int2float_rn(t)), __fsub_rn(km[i], km[i - 1])), dt),
+                          fold[i]);
+        x[i] = v;
+    }
+}
+
+extern "C" int kpstm_finish_noalloc(const kpstm_params *params, const float *d_km, const float *d_fold,
+                                    float *d_out, void *cuda_stream)
+{
+    if (!params || !d_km || !d_fold || !d_out) return KPSTM_ERR_INVALID_ARG;
+    kpstm_setup s;
+    int st = kpstm_setup_of(params, &s);
+    if (st) return st;
+    const int ns = params->ns;
+    const int64_t n = s.dims.out_elems;
+    if (n > KPSTM_NOALLOC_MAX_SAMPLES || ns > KP_NOALLOC_MAX_NS) return KPSTM_ERR_TOO_LARGE;
+    const size_t smem = sizeof(float) * (((2 * (size_t)ns + 3) & ~size_t(3)) + (size_t)ns * KP_LP_ROWS);
+    if (smem > 220 * 1024) return KPSTM_ERR_TOO_LARGE;
+    float *scratch = nullptr;
+    st = noalloc_scratch(&scratch);
+    if (st) return st;
+    float *x = scratch, *h = scratch + KPSTM_NOALLOC_MAX_SAMPLES;
+    /* scalars of create_aliasfilter (Kirchhoff.c:403-412), as kpstm_aliasfilter */
+    const float fs = (float)(2.0 / ((double)params->dt * (double)ns));
+    float fm = (float)params->anti_alias_cutoff;
+    fm = (float)((double)fm * 3.0);
+    const float den = ((fm * fm) * fm) * fm;
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    k_noalloc_impulse<<<(ns + 127) / 128, 128, 0, stream>>>(ns, fs, den, h);
+    KP_CUDA(cudaGetLastError());
+    k_deriv_caller<<<1024, 256, 0, stream>>>(d_km, d_fold, n, ns, params->dt, x);
+    KP_CUDA(cudaGetLastError());
+    KP_CUDA(cudaFuncSetAttribute(k_lowpass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t nrows = n / ns;
+    k_lowpass<<<(unsigned)((nrows + KP_LP_ROWS - 1) / KP_LP_ROWS), 256, smem, stream>>>(x, h, nrows, ns, d_out);
+    KP_CUDA(cudaGetLastError());
     return KPSTM_OK;
 }
