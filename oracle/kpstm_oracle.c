@@ -106,7 +106,7 @@ typedef struct {
     const int *t1;         /* [ns] velocity time index */
     const ko_geom *geom;
     const float *D;        /* [ntr][ns] triangle taps per output index T */
-    const float *P;        /* full mode: [ntr][ns + 2*tm] double running integral */
+    const float *P;        /* full mode: [ntr][ns] the traces' samples */
     int tm, lmax;
     int64_t ntr;
     float *km, *fold;
@@ -116,27 +116,39 @@ typedef struct {
     int err;
 } ko_job;
 
-/* Linear interpolation of the running integral at fractional index x
-   (sample units; P[tm + i] holds index i). */
-static double interp(const float *P, int tm, double x)
+/* Full-physics operator (no counterpart in the reference; the GPU's
+   KPSTM_MODE_FULL), in double.  For image sample t of a column and a trace
+   with source S and receiver R:
+     ts = sqrt((t0/2)^2 + |I-S|^2/v^2), tr likewise, T = (ts + tr)/dt
+     (a pair counts when T < ns - 1),
+     Lf = clamp(1 + |dT/dx| dx + |dT/dy| dy, 1, lmax), the operator's lateral
+     slope in samples per trace spacing,
+     tri = sum_k f[k] max(0, Lf - |T - k|)   (a triangle of real half-width
+     Lf centred on T: what the GPU reads from the double running integral
+     of the trace as [P(T-1+Lf) - 2P(T-1) + P(T-1-Lf)] with linear
+     interpolation and P = 0 before the trace),
+     contribution t0 (1/ts + 1/tr)^2 / 8 * tri / Lf^2.
+   The reference's 1/(t dt)^2 data scaling (Kirchhoff.c:1316) is not used:
+   it puts a factor dt^-2 on the second sample and ruins float running
+   integrals of noisy traces. */
+static double full_tri(const float *f, int ns, double T, double Lf)
 {
-    double fl = floor(x);
-    int i = (int)fl + tm;
-    double fr = x - fl;
-    return (double)P[i] + fr * ((double)P[i + 1] - (double)P[i]);
+    int k0 = (int)ceil(T - Lf), k1 = (int)floor(T + Lf);
+    if (k0 < 0) k0 = 0;
+    if (k1 > ns - 1) k1 = ns - 1;
+    double tri = 0.0;
+    for (int k = k0; k <= k1; ++k) {
+        double w = Lf - fabs(T - k);
+        if (w > 0) tri += (double)f[k] * w;
+    }
+    return tri;
 }
 
-/* Full-physics operator (no counterpart in the reference; the GPU's
-   KPSTM_MODE_FULL), in double: tau = ts + tr with
-   ts = sqrt((t0/2)^2 + |I-S|^2/v^2); a triangle of real half-width
-   Lf = clamp(1 + |dtau/dx| dx/dt + |dtau/dy| dy/dt, 1, lmax) read from the
-   double running integral as [P(T-1+Lf) - 2P(T-1) + P(T-1-Lf)]/Lf^2 at
-   T = tau/dt (linear interpolation); weight t0 (1/ts + 1/tr)^2 / 8. */
 static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, const float *v2,
-                       const float *P, float *k, float *f)
+                       const float *f, float *k, float *fo)
 {
     const kpstm_params *p = J->p;
-    const int ns = J->d->ns, tm = J->tm;
+    const int ns = J->d->ns;
     const double dt = (double)J->d->dt;
     const double sx = (double)IX - g->sxt, sy = (double)IY - g->syt;
     const double gx = (double)IX - g->gxt, gy = (double)IY - g->gyt;
@@ -155,12 +167,10 @@ static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, co
         double slx = (sx / ts + gx / tr) * rv2 * ax, sly = (sy / ts + gy / tr) * rv2 * ay;
         double Lf = 1.0 + fabs(slx) + fabs(sly);
         if (Lf > J->lmax) Lf = J->lmax;
-        double x0 = Tf - 1.0;
-        double tri = (interp(P, tm, x0 + Lf) - 2.0 * interp(P, tm, x0) + interp(P, tm, x0 - Lf)) / (Lf * Lf);
         double u = 1.0 / ts + 1.0 / tr;
-        double w = t0 / 8.0 * u * u;
-        k[t] = (float)((double)k[t] + w * tri);
-        f[t] = f[t] + 1.0f;
+        double w = t0 / 8.0 * u * u / (Lf * Lf);
+        k[t] = (float)((double)k[t] + w * full_tri(f, ns, Tf, Lf));
+        fo[t] = fo[t] + 1.0f;
     }
 }
 
@@ -206,7 +216,7 @@ static void *column_worker(void *arg)
             float *k = km + (size_t)g->off * ns;
             float *f = fold + (size_t)g->off * ns;
             if (p->mode == KPSTM_MODE_FULL) {
-                full_pairs(J, g, IX, IY, v2, J->P + (size_t)it * (ns + 2 * J->tm), k, f);
+                full_pairs(J, g, IX, IY, v2, J->P + (size_t)it * ns, k, f);
                 pairs += ns;
                 continue;
             }
@@ -344,7 +354,7 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
         float dIC = sqrtf((IXc - g->cmpx) * (IXc - g->cmpx) + (IYc - g->cmpy) * (IYc - g->cmpy));
         g->live = (off >= 0 && off < nh) && ((double)dIC < p->aperture + (double)add_on);
         if (g->live && full) {
-            ko_prep_trace(ns, tm, p->dt, t2, samples + (size_t)it * ns, D + (size_t)it * prow);
+            memcpy(D + (size_t)it * ns, samples + (size_t)it * ns, sizeof(float) * ns);
         } else if (g->live) {
             ko_prep_trace(ns, tm, p->dt, t2, samples + (size_t)it * ns, P);
             float *Dt = D + (size_t)it * ns;

@@ -43,6 +43,7 @@ struct kpstm_ctx {
     float2 *d_vrows;
     float *d_t2;
     float2 *d_t2c;
+    float *d_tscale;             /* full mode: per-sample read-out factor t dt/8 */
     double *d_c4, *d_c4r;
     float *d_h;
     float *d_invl2;
@@ -277,8 +278,8 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     a.aperture = p->aperture;
     float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
     a.tile_r2 = r * r;
-    a.aax = (float)(p->iline_distance / p->dt);
-    a.aay = (float)(p->xline_distance / p->dt);
+    a.aax = (float)p->iline_distance; /* slopes in samples per trace spacing (sample units) */
+    a.aay = (float)p->xline_distance;
     int pi = prof_begin(c);
     KP_CUDA(launch_image(c, a));
     prof_end(c, pi, 0, 1);
@@ -306,14 +307,18 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     cudaGetDevice(&c->device);
     const int ns = params->ns, tm = s.dims.trange_max;
     const int ncol = s.ncol;
-    c->nwin = (ns + 1023) / 1024;
+    /* samples per lane: as many as fit the 128-register budget of 2 CTAs/SM
+       without spilling (reference 32, full 24, Kahan variants 8 fewer) */
+    const bool fullm = params->mode == KPSTM_MODE_FULL, kah = params->precision == KPSTM_PREC_BF16_KAHAN;
+    const int kmax = (fullm ? 24 : 32) - (kah ? 8 : 0);
+    c->nwin = (ns + 32 * kmax - 1) / (32 * kmax);
     int per = (ns + c->nwin - 1) / c->nwin;
     c->K = per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
     c->ntile = (ncol + KPSTM_COLS_PER_CTA - 1) / KPSTM_COLS_PER_CTA;
     if (params->mode == KPSTM_MODE_FULL)
         c->row = ((2 * (int64_t)(ns + 2 * tm - 3)) + 3) & ~int64_t(3);
     else
-        c->row = (ns + 3) & ~3;
+        c->row = (ns + 1 + 3) & ~3; /* D[0..ns-1] plus a zero sentinel D[ns] */
 
     /* host tables */
     float *colxy = (float *)malloc(sizeof(float) * 2 * ncol);
@@ -323,6 +328,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     double *c4 = (double *)malloc(sizeof(double) * ns);
     double *c4r = (double *)malloc(sizeof(double) * ns);
     float2 *t2c = (float2 *)malloc(sizeof(float2) * ns);
+    float *tsc = (float *)malloc(sizeof(float) * ns);
     double *hd = (double *)malloc(sizeof(double) * ns);
     float *hf = (float *)malloc(sizeof(float) * ns);
     float4 *box = (float4 *)malloc(sizeof(float4) * c->ntile);
@@ -331,7 +337,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     float invl2[64];
     int nrow = 0;
     do {
-        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !hd || !hf || !box) {
+        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !tsc || !hd || !hf || !box) {
             st = KPSTM_ERR_OUT_OF_MEMORY;
             break;
         }
@@ -341,7 +347,12 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             c4[t] = 4.0 * (double)t2[t];
             c4r[t] = t > 0 ? 1.0 / c4[t] : 0.0;
             double t0 = (double)t * (double)params->dt;
-            t2c[t] = make_float2((float)(0.25 * t0 * t0), (float)(t0 / 8.0));
+            (void)t0;
+            /* full mode works in sample units: (t/2)^2 and t0/(8 dt^2) = t/(8 dt);
+               t = 0 gets a tiny positive time so that rsqrt never sees 0 */
+            t2c[t] = make_float2(t > 0 ? (float)(0.25 * (double)t * (double)t) : 1e-12f,
+                                 (float)((double)t / (8.0 * (double)params->dt)));
+            tsc[t] = (float)((double)t / (8.0 * (double)params->dt)); /* t0/(8 dt^2), sample units */
         }
         st = kpstm_lowpass_kernel(params, hd);
         if (st) break;
@@ -415,6 +426,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             KP_ALLOC(c->d_vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns);
             KP_ALLOC(c->d_t2, sizeof(float) * ns);
             KP_ALLOC(c->d_t2c, sizeof(float2) * ns);
+            if (params->mode == KPSTM_MODE_FULL) KP_ALLOC(c->d_tscale, sizeof(float) * ns);
             KP_ALLOC(c->d_c4, sizeof(double) * ns);
             KP_ALLOC(c->d_c4r, sizeof(double) * ns);
             KP_ALLOC(c->d_h, sizeof(float) * ns);
@@ -434,6 +446,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
                             cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_t2, t2, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_t2c, t2c, sizeof(float2) * ns, cudaMemcpyHostToDevice, c->cs);
+            if (c->d_tscale) cudaMemcpyAsync(c->d_tscale, tsc, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_c4, c4, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_c4r, c4r, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_h, hf, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
@@ -453,6 +466,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     free(c4);
     free(c4r);
     free(t2c);
+    free(tsc);
     free(hd);
     free(hf);
     free(box);
@@ -472,7 +486,7 @@ static int kp_free_all(kpstm_ctx *c)
     if (c->cs) cudaStreamSynchronize(c->cs);
     if (c->own_cs && c->own_cs != c->cs) cudaStreamSynchronize(c->own_cs);
     if (c->xs) cudaStreamSynchronize(c->xs);
-    void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_c4, c->d_c4r,
+    void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_tscale, c->d_c4, c->d_c4r,
                     c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
                     c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
                     c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y};
@@ -611,7 +625,7 @@ static int finish_dev(kpstm_ctx *c, float *out, float *fold)
         int st = ensure_finish_scratch(c);
         if (st) return st;
         int pf = prof_begin(c);
-        k_deriv<<<1024, 256, 0, c->cs>>>(c->d_km, c->d_cnt, ncol, ncls, ns, c->p.dt, c->d_x);
+        k_deriv<<<1024, 256, 0, c->cs>>>(c->d_km, c->d_cnt, c->d_tscale, ncol, ncls, ns, c->p.dt, c->d_x);
         KP_CUDA(cudaGetLastError());
         size_t smem = sizeof(float) * (((2 * (size_t)ns + 3) & ~size_t(3)) + (size_t)ns * KP_LP_ROWS);
         if (smem > 220 * 1024) return KPSTM_ERR_UNSUPPORTED;
@@ -622,7 +636,7 @@ static int finish_dev(kpstm_ctx *c, float *out, float *fold)
         prof_end(c, pf, 2, 2);
     }
     if (fold) {
-        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, ncol, ncls, ns, fold);
+        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, nullptr, ncol, ncls, ns, fold);
         KP_CUDA(cudaGetLastError());
     }
     return KPSTM_OK;
@@ -667,12 +681,12 @@ extern "C" int kpstm_get_accumulators(kpstm_ctx *c, float *km, float *fold)
     const int ns = c->p.ns, ncol = c->s.ncol, ncls = c->s.nclass;
     const size_t bytes = sizeof(float) * (size_t)c->s.dims.out_elems;
     if (km) {
-        k_relayout<<<1024, 256, 0, c->cs>>>(c->d_km, nullptr, ncol, ncls, ns, c->d_x);
+        k_relayout<<<1024, 256, 0, c->cs>>>(c->d_km, nullptr, c->d_tscale, ncol, ncls, ns, c->d_x);
         KP_CUDA(cudaGetLastError());
         KP_CUDA(cudaMemcpyAsync(km, c->d_x, bytes, cudaMemcpyDeviceToHost, c->cs));
     }
     if (fold) {
-        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, ncol, ncls, ns, c->d_y);
+        k_relayout<<<1024, 256, 0, c->cs>>>(nullptr, c->d_cnt, nullptr, ncol, ncls, ns, c->d_y);
         KP_CUDA(cudaGetLastError());
         KP_CUDA(cudaMemcpyAsync(fold, c->d_y, bytes, cudaMemcpyDeviceToHost, c->cs));
     }

@@ -192,14 +192,18 @@ __global__ void __launch_bounds__(1024) k_bucket(const int32_t *cls, int64_t ntr
     }
 }
 
-/* Per-trace running integrals of Kirchhoff.c:1312-1328, one thread per
-   trace, in the reference's order and precision: the first integral adds
-   f[t]/(4*t2[t]) in double and stores float, the tail adds
-   f[ns-1]/(dt*dt*t*t) in float (the fast-math a/(b*c) form of
-   :1320), the second integral is a float running sum, the front is
-   mirrored.  Reference mode stores D[T] = -2P[T] + P[T-2] + P[T+2] summed in
-   double (:1391-1392); full mode stores P over [-tm, ns+tm-2) as pairs
-   {P[i], P[i+1]-P[i]} for linear interpolation. */
+/* Per-trace tap tables, one thread per trace.
+   Reference mode: the running integrals of Kirchhoff.c:1312-1328 in the
+   reference's order and precision - the first integral adds f[t]/(4*t2[t])
+   in double and stores float, the tail adds f[ns-1]/(dt*dt*t*t) in float
+   (the fast-math a/(b*c) form of :1320), the second integral is a float
+   running sum, the front is mirrored - and the taps
+   D[T] = -2P[T] + P[T-2] + P[T+2] summed in double (:1391-1392), plus a zero
+   sentinel D[ns].
+   Full mode: the double running integral P of the unscaled trace (P = 0
+   before the trace, f = 0 after it), accumulated in double and stored over
+   [-tm, ns+tm-4] as pairs {P[i], P[i+1]-P[i]} for linear interpolation
+   (ns + 2tm - 3 entries per row). */
 __global__ void k_prep(KpPrepArgs a)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -213,17 +217,29 @@ __global__ void k_prep(KpPrepArgs a)
     const uint16_t *f16 = a.samples_bf16 ? a.samples_bf16 + (int64_t)src * ns : nullptr;
     const float sc = f16 ? a.scale[src] : 1.0f;
 #define KP_SAMPLE(t) (f32 ? f32[(t)] : __fmul_rn(__uint_as_float(((uint32_t)f16[(t)]) << 16), sc))
+    if (a.full) {
+        float2 *q = reinterpret_cast<float2 *>(row); /* q[i + tm] for P index i */
+        for (int j = tm; j > 1; --j) q[tm - j] = make_float2(0.0f, 0.0f);
+        double p1 = 0.0, p2 = 0.0;
+        /* last P index stored: the imaging kernel reads entry floor(x) + tm with
+           x < ns - 2 + lmax and lmax <= tm - 1, i.e. entries 0 .. ns + 2tm - 4 */
+        const int iend = ns + tm - 4;
+        for (int t = 0; t <= iend + 1; ++t) {
+            if (t < ns) p1 += (double)KP_SAMPLE(t);
+            const double prev = p2;
+            p2 += p1; /* P[t] */
+            q[t - 1 + tm] = make_float2((float)prev, (float)p1); /* entry of P index t-1 */
+        }
+        return;
+    }
     const float flast = KP_SAMPLE(ns - 1);
     const float dt2 = __fmul_rn(a.dt, a.dt);
     float p1 = KP_SAMPLE(0);
     float p2 = p1;
-    /* ring of P2[t-4..t] for the reference taps; P2[1], P2[2] kept for the mirror */
+    /* ring of P2[t-4..t] for the taps; P2[1], P2[2] kept for the mirror */
     float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, r4 = p2;
     float m1 = 0.f, m2 = 0.f;
-    const int tend = a.full ? ns + tm - 2 : ns + 2;
-    float2 *q = reinterpret_cast<float2 *>(row);
-    float prev = p2;
-    for (int t = 1; t < tend; ++t) {
+    for (int t = 1; t < ns + 2; ++t) {
         if (t < ns) {
             double v = __dadd_rn((double)p1, kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]));
             p1 = __double2float_rn(v);
@@ -234,26 +250,15 @@ __global__ void k_prep(KpPrepArgs a)
         p2 = __fadd_rn(p2, p1);
         if (t == 1) m1 = p2;
         if (t == 2) m2 = p2;
-        if (!a.full) {
-            r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = p2; /* r4 = P2[t] */
-            if (t >= 2) {
-                int T = t - 2;
-                float pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
-                double d = __dadd_rn(__dadd_rn(-2.0 * (double)r2, (double)pm), (double)r4);
-                if (T < ns) row[T] = __double2float_rn(d);
-            }
-        } else {
-            q[t - 1 + tm] = make_float2(prev, __fsub_rn(p2, prev)); /* entry for P2[t-1] */
-            prev = p2;
+        r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = p2; /* r4 = P2[t] */
+        if (t >= 2) {
+            int T = t - 2;
+            float pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
+            double d = __dadd_rn(__dadd_rn(-2.0 * (double)r2, (double)pm), (double)r4);
+            if (T < ns) row[T] = __double2float_rn(d);
         }
     }
-    if (a.full) {
-        /* entries for P2[-j], j = 1..tm: {P2[j], P2[j-1] - P2[j]} */
-        for (int j = 1; j <= tm; ++j) {
-            float pj = q[j + tm].x, pj1 = q[j - 1 + tm].x;
-            q[tm - j] = make_float2(pj, __fsub_rn(pj1, pj));
-        }
-    }
+    row[ns] = 0.0f; /* sentinel read for samples whose T >= ns */
 #undef KP_SAMPLE
 }
 
@@ -282,11 +287,17 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     const int ns = a.ns;
     const int64_t row = a.row;
 
-    /* shared layout */
+    /* shared layout (lane l owns samples tw0 + l + 32k):
+       reference (two samples per packed-fp32 instruction, k = 2q and 2q + 1):
+         s_v float4 [8][K/2][32] {v2(t), v2(t+32), -RN(1/v2(t)), -RN(1/v2(t+32))}
+         s_t float2 [K/2][32]    {t2(t), t2(t+32)}            (t2: Kirchhoff.c:1247)
+       full:
+         s_v float2 [8][W]       {(t/2)^2, 1/(v dt)^2}  (sample units: the square
+                                 roots of the DSR terms come out in samples) */
     uint8_t *p = smem;
-    float2 *s_v = reinterpret_cast<float2 *>(p);                 /* ref: [8][W] {v2, rv2}; full: rv2 in .y */
+    float2 *s_v = reinterpret_cast<float2 *>(p);
     p += sizeof(float2) * KPSTM_COLS_PER_CTA * W;
-    float2 *s_t = reinterpret_cast<float2 *>(p);                 /* [W] ref {t2,0} / full {t2, t0/8} */
+    float *s_t = reinterpret_cast<float *>(p);
     p += sizeof(float2) * W;
     float *s_buf = reinterpret_cast<float *>(p);                 /* [2][TB][row] */
     p += sizeof(float) * 2 * TB * row;
@@ -294,23 +305,33 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     p += sizeof(int32_t) * KP_LCH;
     int32_t *s_wsum = reinterpret_cast<int32_t *>(p);            /* [8] */
     p += sizeof(int32_t) * 8;
-    int32_t *s_flag = reinterpret_cast<int32_t *>(p);            /* [2]: abort, hits */
+    int32_t *s_flag = reinterpret_cast<int32_t *>(p);            /* [2]: abort, spare */
     p += sizeof(int32_t) * 2;
     p = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
     uint64_t *s_bar = reinterpret_cast<uint64_t *>(p);           /* [2] */
 
     const int vrow = colok ? a.colrow[col] : -1;
-    for (int t = lane; t < W; t += 32) {
-        int tt = tw0 + t;
-        float2 v = make_float2(1.0f, 1.0f);
-        if (vrow >= 0 && tt < ns) v = a.vrows[(int64_t)vrow * ns + tt];
-        s_v[w * W + t] = v;
-    }
-    for (int t = tid; t < W; t += KP_THREADS) {
-        int tt = tw0 + t;
-        float2 v = make_float2(0.0f, 0.0f);
-        if (tt < ns) v = FULL ? a.t2c[tt] : make_float2(a.t2[tt], 0.0f);
-        s_t[t] = v;
+    const float rdt2 = a.rdt * a.rdt;
+    if (FULL) {
+        for (int t = lane; t < W; t += 32) {
+            const int tt = tw0 + t;
+            float2 v = make_float2(1.0f, 1.0f);
+            if (vrow >= 0 && tt < ns) v = a.vrows[(int64_t)vrow * ns + tt];
+            s_v[w * W + t] = make_float2(tt < ns ? a.t2c[tt].x : 1.0f, v.y * rdt2);
+        }
+    } else {
+        for (int i = lane; i < (K / 2) * 32; i += 32) {
+            const int q = i >> 5, l = i & 31;
+            const int ta = tw0 + l + 64 * q, tb = ta + 32;
+            float2 va = make_float2(1.0f, 1.0f), vb = make_float2(1.0f, 1.0f);
+            if (vrow >= 0 && ta < ns) va = a.vrows[(int64_t)vrow * ns + ta];
+            if (vrow >= 0 && tb < ns) vb = a.vrows[(int64_t)vrow * ns + tb];
+            reinterpret_cast<float4 *>(s_v)[(w * (K / 2) + q) * 32 + l] = make_float4(va.x, vb.x, -va.y, -vb.y);
+        }
+        for (int i = tid; i < (K / 2) * 32; i += KP_THREADS) {
+            const int ta = tw0 + (i & 31) + 64 * (i >> 5), tb = ta + 32;
+            reinterpret_cast<float2 *>(s_t)[i] = make_float2(ta < ns ? a.t2[ta] : 0.0f, tb < ns ? a.t2[tb] : 0.0f);
+        }
     }
     if (tid == 0) {
         kp_mbar_init(&s_bar[0], 1);
@@ -324,14 +345,21 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     const float4 box = a.tilebox[blockIdx.x];
     const int64_t obase = ((int64_t)cls * a.ncol + (colok ? col : 0)) * ns + tw0 + lane;
 
-    float acc[K], comp[KAHAN ? K : 1];
+    /* accumulators as sample pairs: acc[q] = samples 2q (x) and 2q + 1 (y), i.e.
+       tw0 + lane + 64q and + 32 */
+    float2 acc[K / 2], comp[KAHAN ? K / 2 : 1];
     int cnt[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        int tt = tw0 + lane + 32 * k;
-        acc[k] = (colok && tt < ns) ? a.km[obase + 32 * k] : 0.0f;
-        if (KAHAN) comp[k] = (colok && tt < ns) ? a.kc[obase + 32 * k] : 0.0f;
-        cnt[k] = 0;
+    for (int q = 0; q < K / 2; ++q) {
+        const int ta = tw0 + lane + 64 * q, tb = ta + 32;
+        acc[q].x = (colok && ta < ns) ? a.km[obase + 64 * q] : 0.0f;
+        acc[q].y = (colok && tb < ns) ? a.km[obase + 64 * q + 32] : 0.0f;
+        if (KAHAN) {
+            comp[q].x = (colok && ta < ns) ? a.kc[obase + 64 * q] : 0.0f;
+            comp[q].y = (colok && tb < ns) ? a.kc[obase + 64 * q + 32] : 0.0f;
+        }
+        cnt[2 * q] = 0;
+        cnt[2 * q + 1] = 0;
     }
     __syncthreads();
 
@@ -340,6 +368,7 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     uint32_t nb = 0; /* batches issued so far (buffer = nb & 1) */
     int my_hits = 0;
     bool abort = false;
+    const float tmax = a.nsf - 1.0f;
 
     for (int c0 = cb; c0 < ce && !abort; c0 += KP_LCH) {
         /* order-preserving compaction of the chunk's traces that can reach
@@ -404,73 +433,87 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
                     const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
                     const float *tab = s_buf + ((nb & 1) * TB + (j - j0)) * row;
                     const float2 *sv = s_v + w * W + lane;
-                    const float2 *st = s_t + lane;
                     if (!FULL) {
+                        const float4 *sv4 = reinterpret_cast<const float4 *>(s_v) + w * (K / 2) * 32 + lane;
+                        const float2 *st2 = reinterpret_cast<const float2 *>(s_t) + lane;
+                        const float2 nS = kp_bc2(-dIS2), nR = kp_bc2(-dIR2);
+                        const float2 dt2 = kp_bc2(a.dt), nrdt2 = kp_bc2(-a.rdt);
+                        const float nnsf = -a.nsf;
 #pragma unroll
-                        for (int k = 0; k < K; ++k) {
-                            const float2 vr = sv[32 * k];
-                            const float t2 = st[32 * k].x;
-                            float s1 = __fadd_rn(t2, kp_div_rn(dIS2, vr.x, vr.y));
-                            float s2 = __fadd_rn(t2, kp_div_rn(dIR2, vr.x, vr.y));
-                            float S = kp_dsqrt_sum(s1, s2);
-                            float qq = kp_div_rn(S, a.dt, a.rdt); /* dsr/dt, :1384 */
-                            if (qq < a.nsf) {                    /* T < ns, :1387 */
-                                int T = kp_floor_bits(qq) - KP_MAGIC_BITS;
-                                float d = tab[T];
-                                if (KAHAN) {
-                                    float y = __fsub_rn(d, comp[k]);
-                                    float s = __fadd_rn(acc[k], y);
-                                    comp[k] = __fsub_rn(__fsub_rn(s, acc[k]), y);
-                                    acc[k] = s;
-                                } else {
-                                    acc[k] = __fadd_rn(acc[k], d);
-                                }
-                                cnt[k] += 1;
+                        for (int q = 0; q < K / 2; ++q) {
+                            const float4 vv = sv4[32 * q];
+                            const float2 t2 = st2[32 * q];
+                            const float2 v2 = make_float2(vv.x, vv.y), nr = make_float2(vv.z, vv.w);
+                            /* RN(d/v^2): q = (-d)(-1/v^2); e' = q v^2 - d; q + e'(-1/v^2) */
+                            float2 q1 = __fmul2_rn(nS, nr);
+                            q1 = __ffma2_rn(__ffma2_rn(q1, v2, nS), nr, q1);
+                            float2 q2 = __fmul2_rn(nR, nr);
+                            q2 = __ffma2_rn(__ffma2_rn(q2, v2, nR), nr, q2);
+                            const float2 S = kp_dsqrt_sum2(__fadd2_rn(t2, q1), __fadd2_rn(t2, q2));
+                            /* -RN(S/dt) (Kirchhoff.c:1384): nq = S(-1/dt); e = S + nq dt; nq + e(-1/dt) */
+                            float2 nq = __fmul2_rn(S, nrdt2);
+                            nq = __ffma2_rn(__ffma2_rn(nq, dt2, S), nrdt2, nq);
+                            /* floor(RN(S/dt)): -(q + 1.5*2^23) toward zero; its bits minus
+                               0xCB400000 (sign + magic) are T; T >= ns reads the zero D[ns] */
+                            const float2 fb = __fadd2_rz(nq, kp_bc2(-KP_MAGIC));
+                            const bool va = nq.x > nnsf, vb = nq.y > nnsf; /* T < ns, :1387 */
+                            const int ia = va ? (int)((uint32_t)__float_as_int(fb.x) - 0xCB400000u) : ns;
+                            const int ib = vb ? (int)((uint32_t)__float_as_int(fb.y) - 0xCB400000u) : ns;
+                            const float2 d = make_float2(tab[ia], tab[ib]);
+                            if (KAHAN) {
+                                const float2 y = __fadd2_rn(d, kp_neg2(comp[q]));
+                                const float2 s = __fadd2_rn(acc[q], y);
+                                comp[q] = __fadd2_rn(__fadd2_rn(s, kp_neg2(acc[q])), kp_neg2(y));
+                                acc[q] = s;
+                            } else {
+                                acc[q] = __fadd2_rn(acc[q], d); /* + 0 where T >= ns: exact no-op */
                             }
+                            cnt[2 * q] += va;
+                            cnt[2 * q + 1] += vb;
                         }
                     } else {
-                        /* full physics: tau = ts + tr, ts = sqrt(t0^2/4 + |I-S|^2/v^2);
-                           a triangle of real half-width Lf (1 + the operator's lateral
-                           slope in samples per trace spacing, <= lmax) read from the
-                           double running integral at three fractional positions;
-                           weight t0 (1/ts + 1/tr)^2 / 8 */
+                        /* full physics in sample units: a = (t/2)^2 + |I-S|^2/(v dt)^2,
+                           Tf = sqrt(a_s) + sqrt(a_r); a triangle of real half-width Lf
+                           (1 + the operator's lateral slope in samples per trace
+                           spacing, <= lmax) read from the double running integral at
+                           three fractional positions; weight t0 (1/ts + 1/tr)^2 / 8
+                           divided by Lf^2, of which (1/ts' + 1/tr')^2 / Lf^2 is applied
+                           here and the per-sample factor t0 / (8 dt^2) when the
+                           accumulators are read (ts' = ts/dt) */
                         const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
                         const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
                         /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm */
                         const float2 *q2 = reinterpret_cast<const float2 *>(tab) + a.tm;
 #pragma unroll
                         for (int k = 0; k < K; ++k) {
-                            const float rv2 = sv[32 * k].y;
-                            const float2 tc = st[32 * k];
-                            float as = fmaxf(fmaf(dIS2, rv2, tc.x), 1e-30f);
-                            float ar = fmaxf(fmaf(dIR2, rv2, tc.x), 1e-30f);
-                            float rs = kp_rsqrt_approx(as), rr = kp_rsqrt_approx(ar);
-                            float Tf = fmaf(as, rs, ar * rr) * a.rdt;
-                            if (Tf < a.nsf - 1.0f) {
-                                float gxx = fmaf(axs, rs, axr * rr), gyy = fmaf(ays, rs, ayr * rr);
-                                float Lf = fminf(fmaf(fabsf(gxx) + fabsf(gyy), rv2, 1.0f), a.lmaxf);
-                                float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
-                                int b0 = kp_floor_bits(x0), ba = kp_floor_bits(xa), bb = kp_floor_bits(xb);
-                                float f0 = x0 - (__int_as_float(b0) - KP_MAGIC);
-                                float fa = xa - (__int_as_float(ba) - KP_MAGIC);
-                                float fb = xb - (__int_as_float(bb) - KP_MAGIC);
-                                float2 q0 = q2[b0 - KP_MAGIC_BITS], qa = q2[ba - KP_MAGIC_BITS], qb = q2[bb - KP_MAGIC_BITS];
-                                /* second difference without cancellation: table
-                                   differences (exact for neighbouring values) plus the
-                                   small interpolation terms */
-                                float big = (qa.x - q0.x) + (qb.x - q0.x);
-                                float small = fmaf(-2.0f * f0, q0.y, fmaf(fa, qa.y, fb * qb.y));
-                                float il = kp_rcp_approx(Lf);
-                                float tri = (big + small) * (il * il);
-                                float u = rs + rr;
-                                float wgt = tc.y * u * u;
+                            const float2 tv = sv[32 * k]; /* sample tw0 + lane + 32k */
+                            const float as = fmaf(dIS2, tv.y, tv.x), ar = fmaf(dIR2, tv.y, tv.x);
+                            const float rs = kp_rsqrt_approx(as), rr = kp_rsqrt_approx(ar);
+                            const float Tf = fmaf(as, rs, ar * rr);
+                            if (Tf < tmax) { /* late samples of far traces skip the taps (whole warps) */
+                                const float gxx = fmaf(axs, rs, axr * rr), gyy = fmaf(ays, rs, ayr * rr);
+                                const float Lf = fminf(fmaf(fabsf(gxx) + fabsf(gyy), tv.y, 1.0f), a.lmaxf);
+                                const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
+                                const int b0 = kp_floor_bits(x0), ba = kp_floor_bits(xa), bb = kp_floor_bits(xb);
+                                const float f0 = x0 - (__int_as_float(b0) - KP_MAGIC);
+                                const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
+                                const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
+                                const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
+                                const float2 Qb = q2[bb - KP_MAGIC_BITS];
+                                /* second difference without cancellation: table differences
+                                   (exact for neighbouring values) plus the interpolation terms */
+                                const float big = (Qa.x - Q0.x) + (Qb.x - Q0.x);
+                                const float small = fmaf(fa, Qa.y, fb * Qb.y) - 2.0f * (f0 * Q0.y);
+                                const float ui = (rs + rr) * kp_rcp_approx(Lf);
+                                float &ak = (k & 1) ? acc[k >> 1].y : acc[k >> 1].x;
                                 if (KAHAN) {
-                                    float y = fmaf(wgt, tri, -comp[k]);
-                                    float s = acc[k] + y;
-                                    comp[k] = (s - acc[k]) - y;
-                                    acc[k] = s;
+                                    float &ck = (k & 1) ? comp[k >> 1].y : comp[k >> 1].x;
+                                    float y = fmaf(ui * ui, big + small, -ck);
+                                    float s = ak + y;
+                                    ck = (s - ak) - y;
+                                    ak = s;
                                 } else {
-                                    acc[k] = fmaf(wgt, tri, acc[k]);
+                                    ak = fmaf(ui * ui, big + small, ak);
                                 }
                                 cnt[k] += 1;
                             }
@@ -488,12 +531,17 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     if (abort) return;
     if (colok) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            int tt = tw0 + lane + 32 * k;
-            if (tt < ns) {
-                a.km[obase + 32 * k] = acc[k];
-                if (KAHAN) a.kc[obase + 32 * k] = comp[k];
-                a.cnt[obase + 32 * k] += cnt[k];
+        for (int q = 0; q < K / 2; ++q) {
+            const int ta = tw0 + lane + 64 * q, tb = ta + 32;
+            if (ta < ns) {
+                a.km[obase + 64 * q] = acc[q].x;
+                if (KAHAN) a.kc[obase + 64 * q] = comp[q].x;
+                a.cnt[obase + 64 * q] += cnt[2 * q];
+            }
+            if (tb < ns) {
+                a.km[obase + 64 * q + 32] = acc[q].y;
+                if (KAHAN) a.kc[obase + 64 * q + 32] = comp[q].y;
+                a.cnt[obase + 64 * q + 32] += cnt[2 * q + 1];
             }
         }
     }
@@ -503,7 +551,8 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
 /* ------------------------------------------------------------------------ */
 /* Finishing, Kirchhoff.c:1457-1462: x[t] = -dt*t*(km[t]-km[t-1])*dt/fold[t]
    in float, x[0] = 0; rows written in output order [col][cls]. */
-__global__ void k_deriv(const float *km, const int32_t *cnt, int ncol, int ncls, int ns, float dt, float *x)
+__global__ void k_deriv(const float *km, const int32_t *cnt, const float *tscale, int ncol, int ncls, int ns,
+                        float dt, float *x)
 {
     const int64_t n = (int64_t)ncls * ncol * ns;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -513,7 +562,12 @@ __global__ void k_deriv(const float *km, const int32_t *cnt, int ncol, int ncls,
         float v = 0.0f;
         if (t > 0) {
             float fold = __int2float_rn(cnt[i] + 1);
-            v = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(-dt, __int2float_rn(t)), __fsub_rn(km[i], km[i - 1])), dt), fold);
+            float k1 = km[i], k0 = km[i - 1];
+            if (tscale) { /* full mode: the factor t dt/8 kept out of the accumulation */
+                k1 = __fmul_rn(k1, tscale[t]);
+                k0 = __fmul_rn(k0, tscale[t - 1]);
+            }
+            v = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(-dt, __int2float_rn(t)), __fsub_rn(k1, k0)), dt), fold);
         }
         x[((int64_t)col * ncls + cls) * ns + t] = v;
     }
@@ -561,15 +615,17 @@ __global__ void __launch_bounds__(256) k_lowpass(const float *x, const float *h,
     }
 }
 
-/* [cls][col][ns] -> [col][cls][ns]; fold = 1 + count when cnt is given. */
-__global__ void k_relayout(const float *src, const int32_t *cnt, int ncol, int ncls, int ns, float *dst)
+/* [cls][col][ns] -> [col][cls][ns]; fold = 1 + count when cnt is given;
+   src scaled per sample by tscale when given (full mode). */
+__global__ void k_relayout(const float *src, const int32_t *cnt, const float *tscale, int ncol, int ncls, int ns,
+                           float *dst)
 {
     const int64_t n = (int64_t)ncls * ncol * ns;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int64_t r = i / ns;
         int t = (int)(i - r * ns);
         int cls = (int)(r / ncol), col = (int)(r - (int64_t)cls * ncol);
-        float v = cnt ? __int2float_rn(cnt[i] + 1) : src[i];
+        float v = cnt ? __int2float_rn(cnt[i] + 1) : (tscale ? __fmul_rn(src[i], tscale[t]) : src[i]);
         dst[((int64_t)col * ncls + cls) * ns + t] = v;
     }
 }
