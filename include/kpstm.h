@@ -201,6 +201,29 @@ typedef struct {
 int kpstm_profile_enable(kpstm_ctx *ctx, int enable);
 int kpstm_profile_read(kpstm_ctx *ctx, kpstm_profile *out);
 
+/* ---- least-squares migration ------------------------------------------------ */
+/* No counterpart in the reference.  The operator pair is the full-physics
+   migration without its finishing: L^T (migration) maps data d[ntr][ns] to
+   the image accumulators m[nx][ny][nh][ns] (the values
+   kpstm_get_accumulators would return), L (demigration) is its exact
+   transpose.  The context must be created with KPSTM_MODE_FULL.  Data and
+   model vectors are device pointers; data traces follow the order of the
+   headers given to kpstm_lsm_geometry. */
+
+/* Fix the acquisition geometry (ntr trace headers, big-endian words, host). */
+int kpstm_lsm_geometry(kpstm_ctx *ctx, const int32_t *hdr_be, int64_t ntr);
+/* Migration: d_model = L^T d_data. */
+int kpstm_lsm_adjoint(kpstm_ctx *ctx, const float *d_data, float *d_model);
+/* Demigration: d_data = L d_model (traces outside every class or the slab
+   cull get zeros). */
+int kpstm_lsm_forward(kpstm_ctx *ctx, const float *d_model, float *d_data);
+/* Conjugate gradients on min ||L m - d||^2 (CGLS) from m = 0, niter
+   iterations, dot products and step lengths in FP64.  With
+   KPSTM_PREC_BF16_KAHAN the data-domain vectors (d, residual) are stored
+   as bf16 with a per-trace scale.  resid (nullable, niter + 1 values)
+   receives ||d - L m_k||. */
+int kpstm_lsm_cg(kpstm_ctx *ctx, const float *d_data, int32_t niter, float *d_model, double *resid);
+
 /* ---- finishing without device allocation ------------------------------------ */
 
 /* Largest image (nx*ny*nh*ns samples) kpstm_finish_noalloc accepts. */

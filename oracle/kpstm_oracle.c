@@ -397,3 +397,116 @@ done:
     free(vel2); free(t2); free(t1); free(geom); free(D); free(P); free(km); free(fold);
     return st;
 }
+
+/* Least-squares operator pair (full physics, see full_pairs), in double.
+   The pair set and the geometry follow ko_kirchhoff exactly; every pair
+   couples data sample k of the trace with model sample t of the column by
+   t0 (1/ts + 1/tr)^2 / (8 Lf^2) * max(0, Lf - |T - k|). */
+int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be, int64_t ntr,
+                 int direction, const double *in, double *out)
+{
+    if (!p || !v || !hdr_be || !in || !out || ntr <= 0) return KPSTM_ERR_INVALID_ARG;
+    if (p->mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED;
+    ko_dims d;
+    int st = ko_dims_of(p, &d);
+    if (st) return st;
+    const int ns = d.ns, nh = d.nh;
+    int tm;
+    ko_aliasfilter(ns, p->dt, p->iline_distance, p->xline_distance, p->anti_alias_cutoff, &tm, NULL);
+    if (tm < 2) return KPSTM_ERR_TRANGE;
+    int lmax = p->aa_max_halfwidth > 0 ? p->aa_max_halfwidth : tm - 1;
+    if (lmax > tm - 1) lmax = tm - 1;
+    if (lmax > 63) lmax = 63;
+    if (lmax < 1) lmax = 1;
+    const size_t nmod = (size_t)d.nx * d.ny * nh * ns;
+    if (direction == 0) memset(out, 0, sizeof(double) * nmod);
+    else memset(out, 0, sizeof(double) * (size_t)ntr * ns);
+    int *t1 = (int *)malloc(sizeof(int) * ns);
+    if (!t1) return KPSTM_ERR_OUT_OF_MEMORY;
+    for (int t = 0; t < ns; ++t) {
+        int q = (int)round((double)((float)t * (p->dt / v->dtm)));
+        t1[t] = q > v->nsm - 1 ? v->nsm - 1 : q;
+    }
+    float IXc = (float)((p->start_iline + ((d.nx / 2.0 + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance);
+    float IYc = (float)((p->start_xline + ((d.ny / 2.0 + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance);
+    float add_on = (float)(0.5 * sqrt(d.nx * p->inc_iline * p->iline_distance * d.nx * p->inc_iline * p->iline_distance +
+                                      d.ny * p->inc_xline * p->xline_distance * d.ny * p->inc_xline * p->xline_distance));
+    const double dt = (double)p->dt;
+    const double ax = p->iline_distance / dt, ay = p->xline_distance / dt;
+    for (int64_t it = 0; it < ntr && !st; ++it) {
+        const int32_t *h = hdr_be + (size_t)it * 60;
+        double w4[4];
+        for (int k = 0; k < 4; ++k) w4[k] = (double)be32(h[18 + k]) - (k % 2 == 0 ? p->ox : p->oy);
+        ko_geom g;
+        int i = (int)w4[0], j = (int)w4[1];
+        g.sxt = d.cosA * (float)i + d.sinA * (float)j;
+        g.syt = -d.sinA * (float)i + d.cosA * (float)j;
+        i = (int)w4[2];
+        j = (int)w4[3];
+        g.gxt = d.cosA * (float)i + d.sinA * (float)j;
+        g.gyt = -d.sinA * (float)i + d.cosA * (float)j;
+        float h2 = (float)(0.25 * (double)((g.sxt - g.gxt) * (g.sxt - g.gxt) + (g.syt - g.gyt) * (g.syt - g.gyt)));
+        g.cmpx = (float)(0.5 * (double)(g.sxt + g.gxt));
+        g.cmpy = (float)(0.5 * (double)(g.syt + g.gyt));
+        int off = (int)floor((2.0 * sqrt((double)h2) - p->oh) / p->dh);
+        if (!(off >= 0 && off < p->nh)) continue;
+        if (p->output == KPSTM_OUT_STACK) off = 0;
+        float dIC = sqrtf((IXc - g.cmpx) * (IXc - g.cmpx) + (IYc - g.cmpy) * (IYc - g.cmpy));
+        if (!((double)dIC < p->aperture + (double)add_on)) continue;
+        for (int xc = 0; xc < d.nx; ++xc) {
+            for (int yc = 0; yc < d.ny; ++yc) {
+                float IX = (float)((p->start_iline + ((xc + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance);
+                float IY = (float)((p->start_xline + ((yc + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance);
+                float cdx = IX - g.cmpx, cdy = IY - g.cmpy;
+                float dC = sqrtf(cdx * cdx + cdy * cdy);
+                if (!((double)dC < p->aperture)) continue;
+                int xc1 = (int)round((p->start_iline - v->o_iline) / v->d_iline +
+                                     (xc + d.xslice * d.nx) * (p->inc_iline / v->d_iline));
+                int yc1 = (int)round((p->start_xline - v->o_xline) / v->d_xline +
+                                     (yc + d.yslice * d.ny) * (p->inc_xline / v->d_xline));
+                if (xc1 > v->n_iline - 1) xc1 = v->n_iline - 1;
+                if (yc1 > v->n_xline - 1) yc1 = v->n_xline - 1;
+                if (xc1 < 0 || yc1 < 0) { st = KPSTM_ERR_VELOCITY_RANGE; break; }
+                const float *vr = v->vrms + ((size_t)xc1 * v->n_xline + yc1) * v->nsm;
+                const double sx = (double)IX - g.sxt, sy = (double)IY - g.syt;
+                const double gx = (double)IX - g.gxt, gy = (double)IY - g.gyt;
+                const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
+                const size_t mbase = (((size_t)xc * d.ny + yc) * nh + off) * ns;
+                const size_t dbase = (size_t)it * ns;
+                for (int t = 1; t < ns; ++t) {
+                    float vf = vr[t1[t]];
+                    double rv2 = 1.0 / (double)(vf * vf);
+                    double t0 = (double)t * dt;
+                    double th2 = 0.25 * t0 * t0;
+                    double ts = sqrt(th2 + dS2 * rv2), tr = sqrt(th2 + dR2 * rv2);
+                    double T = (ts + tr) / dt;
+                    if (!(T < ns - 1)) continue;
+                    double Lf = 1.0 + fabs((sx / ts + gx / tr) * rv2 * ax) + fabs((sy / ts + gy / tr) * rv2 * ay);
+                    if (Lf > lmax) Lf = lmax;
+                    double u = 1.0 / ts + 1.0 / tr;
+                    double W = t0 / 8.0 * u * u / (Lf * Lf);
+                    int k0 = (int)ceil(T - Lf), k1 = (int)floor(T + Lf);
+                    if (k0 < 0) k0 = 0;
+                    if (k1 > ns - 1) k1 = ns - 1;
+                    if (direction == 0) {
+                        double tri = 0.0;
+                        for (int k = k0; k <= k1; ++k) {
+                            double wk = Lf - fabs(T - k);
+                            if (wk > 0) tri += in[dbase + k] * wk;
+                        }
+                        out[mbase + t] += W * tri;
+                    } else {
+                        double mv = W * in[mbase + t];
+                        for (int k = k0; k <= k1; ++k) {
+                            double wk = Lf - fabs(T - k);
+                            if (wk > 0) out[dbase + k] += mv * wk;
+                        }
+                    }
+                }
+            }
+            if (st) break;
+        }
+    }
+    free(t1);
+    return st;
+}

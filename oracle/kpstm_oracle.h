@@ -51,6 +51,12 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
                  const float *samples, int64_t ntr, float *km, float *fold, float *image,
                  int nthreads, int64_t *pairs);
 
+/* Least-squares operator pair of the full-physics mode, in double:
+   direction 0: model = L^T data (migration, [nx][ny][nh][ns], no fold);
+   direction 1: data = L model (demigration, [ntr][ns]), its exact transpose. */
+int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be, int64_t ntr,
+                 int direction, const double *in, double *out);
+
 /* Finishing only (Kirchhoff.c:1440-1479) of given accumulators. */
 int ko_finish(const kpstm_params *p, const float *km, const float *fold, float *image);
 

@@ -51,6 +51,9 @@ def lib() -> C.CDLL:
         _lib.ko_aliasfilter.restype = C.c_int
         _lib.ko_aliasfilter.argtypes = [C.c_int, C.c_float, C.c_double, C.c_double, C.c_double,
                                         C.POINTER(C.c_int), C.c_void_p]
+        _lib.ko_lsm_apply.restype = C.c_int
+        _lib.ko_lsm_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p,
+                                      C.c_void_p]
         _lib.ko_prep_trace.restype = None
         _lib.ko_prep_trace.argtypes = [C.c_int, C.c_int, C.c_float, f32p, f32p, f32p]
     return _lib
@@ -100,3 +103,23 @@ def kirchhoff(survey, params: dict | None = None, nthreads: int = 0, want_acc: b
     shape = dims["shape"]
     return dict(image=image.reshape(shape), km=None if km is None else km.reshape(shape),
                 fold=None if fold is None else fold.reshape(shape), pairs=pairs.value)
+
+
+def lsm_apply(survey, direction: int, vec: np.ndarray, params: dict | None = None) -> np.ndarray:
+    """Full-mode least-squares operators in double: direction 0 = L^T
+    (data [ntr, ns] -> model [nx, ny, nh, ns]), 1 = L (model -> data)."""
+    from random_gb300 import capi, segy
+    p = dict(survey.params)
+    if params:
+        p.update(params)
+    prm = capi.make_params(p)
+    vel, _keep = capi.make_velocity(survey.velocity)
+    dims = capi.oracle_dims(p)
+    hdr = np.ascontiguousarray(segy.headers_be(survey.headers))
+    src = np.ascontiguousarray(vec, dtype=np.float64)
+    out = np.zeros(dims["shape"] if direction == 0 else (survey.ntr, survey.ns), np.float64)
+    st = lib().ko_lsm_apply(C.addressof(prm), C.addressof(vel), hdr.ctypes.data, survey.ntr, direction,
+                            src.ctypes.data, out.ctypes.data)
+    if st:
+        raise RuntimeError(f"ko_lsm_apply: status {st}")
+    return out

@@ -66,6 +66,13 @@ struct kpstm_ctx {
     unsigned long long *d_hits;
     /* finishing scratch */
     float *d_x, *d_y;
+    /* least-squares migration state */
+    int64_t lsm_ntr, lsm_nlive, lrow;
+    kpstm_geom *d_lgraw, *d_lgeom;
+    int32_t *d_lcls, *d_lorder, *d_lcstart, *d_lnlive, *d_lcnt;
+    float *d_ltable, *d_lkm;
+    unsigned long long *d_lhits;
+    double *d_dotpart, *d_dot;
     /* stream handling / profiling */
     cudaStream_t own_cs;
     int prof;
@@ -489,7 +496,9 @@ static int kp_free_all(kpstm_ctx *c)
     void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_tscale, c->d_c4, c->d_c4r,
                     c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
                     c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
-                    c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y};
+                    c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
+                    c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
+                    c->d_lhits, c->d_dotpart, c->d_dot};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
@@ -881,4 +890,346 @@ extern "C" int kpstm_finish_noalloc(const kpstm_params *params, const float *d_k
     k_lowpass<<<(unsigned)((nrows + KP_LP_ROWS - 1) / KP_LP_ROWS), 256, smem, stream>>>(x, h, nrows, ns, d_out);
     KP_CUDA(cudaGetLastError());
     return KPSTM_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Least-squares migration (kpstm_lsm_*). */
+
+static KpImageArgs image_args(const kpstm_ctx *c)
+{
+    const kpstm_params *p = &c->p;
+    const kpstm_setup *s = &c->s;
+    KpImageArgs a;
+    memset(&a, 0, sizeof(a));
+    a.colxy = c->d_colxy;
+    a.colrow = c->d_colrow;
+    a.tilebox = c->d_tilebox;
+    a.vrows = c->d_vrows;
+    a.t2 = c->d_t2;
+    a.t2c = c->d_t2c;
+    a.inv_l2 = c->d_invl2;
+    a.status = c->d_status;
+    a.ncol = s->ncol;
+    a.ns = p->ns;
+    a.tm = s->dims.trange_max;
+    a.lmax = s->lmax;
+    a.lmaxf = (float)s->lmax;
+    a.dt = p->dt;
+    a.rdt = 1.0f / p->dt;
+    a.nsf = (float)p->ns;
+    a.aperture = p->aperture;
+    float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
+    a.tile_r2 = r * r;
+    a.aax = (float)p->iline_distance;
+    a.aay = (float)p->xline_distance;
+    return a;
+}
+
+template <int K>
+static cudaError_t launch_image_hilo_k(const kpstm_ctx *c, const KpImageArgs &a, dim3 grid, size_t smem)
+{
+    void (*fn)(KpImageArgs) = k_image<K, true, false, true>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, KP_THREADS, smem, c->cs>>>(a);
+    return cudaGetLastError();
+}
+
+static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d_data16, const float *d_scale,
+                            float *d_model)
+{
+    const int ns = c->p.ns, ncol = c->s.ncol, ncls = c->s.nclass;
+    const size_t nimg = (size_t)ncls * ncol * ns;
+    KP_CUDA(cudaMemsetAsync(c->d_lkm, 0, sizeof(float) * nimg, c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_lcnt, 0, sizeof(int32_t) * nimg, c->cs));
+    if (c->lsm_nlive > 0) {
+        KpPrepArgs pa;
+        memset(&pa, 0, sizeof(pa));
+        pa.samples = d_data;
+        pa.samples_bf16 = d_data16;
+        pa.scale = d_scale;
+        pa.geom_raw = c->d_lgraw;
+        pa.order = c->d_lorder;
+        pa.nlive = c->d_lnlive;
+        pa.geom = c->d_lgeom;
+        pa.table = c->d_ltable;
+        pa.c4 = c->d_c4;
+        pa.c4r = c->d_c4r;
+        pa.row = c->lrow;
+        pa.ns = ns;
+        pa.tm = c->s.dims.trange_max;
+        pa.full = 1;
+        pa.hilo = 1;
+        pa.dt = c->p.dt;
+        k_prep<<<(unsigned)((c->lsm_nlive + 127) / 128), 128, 0, c->cs>>>(pa);
+        KP_CUDA(cudaGetLastError());
+        KpImageArgs a = image_args(c);
+        a.geom = c->d_lgeom;
+        a.class_start = c->d_lcstart;
+        a.table = c->d_ltable;
+        a.row = c->lrow;
+        a.km = c->d_lkm;
+        a.cnt = c->d_lcnt;
+        a.hits = c->d_lhits;
+        const int W = 32 * c->K;
+        size_t smem = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W +
+                      sizeof(float) * 2 * KP_TB_FULL * c->lrow + sizeof(int32_t) * (KP_LCH + 8 + 2);
+        smem = ((smem + 7) & ~size_t(7)) + 2 * sizeof(uint64_t);
+        dim3 grid(c->ntile, ncls, c->nwin);
+        cudaError_t e;
+        switch (c->K) {
+        case 8: e = launch_image_hilo_k<8>(c, a, grid, smem); break;
+        case 16: e = launch_image_hilo_k<16>(c, a, grid, smem); break;
+        default: e = launch_image_hilo_k<24>(c, a, grid, smem); break;
+        }
+        KP_CUDA(e);
+    }
+    k_relayout<<<1024, 256, 0, c->cs>>>(c->d_lkm, nullptr, c->d_tscale, ncol, ncls, ns, d_model);
+    KP_CUDA(cudaGetLastError());
+    return KPSTM_OK;
+}
+
+static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
+{
+    const int ns = c->p.ns;
+    KP_CUDA(cudaMemsetAsync(d_data, 0, sizeof(float) * (size_t)c->lsm_ntr * ns, c->cs));
+    if (c->lsm_nlive == 0) return KPSTM_OK;
+    const kpstm_params *p = &c->p;
+    const kpstm_setup *s = &c->s;
+    KpDemigArgs a;
+    memset(&a, 0, sizeof(a));
+    a.geom = c->d_lgeom;
+    a.nlive = c->d_lnlive;
+    a.model = d_model;
+    a.tscale = c->d_tscale;
+    a.colxy = c->d_colxy;
+    a.colrow = c->d_colrow;
+    a.vrows = c->d_vrows;
+    a.t2c = c->d_t2c;
+    a.out = d_data;
+    a.status = c->d_status;
+    a.nx = s->dims.nx;
+    a.ny = s->dims.ny;
+    a.ncls = s->nclass;
+    a.ns = ns;
+    a.ax0 = (float)((p->start_iline + (s->xslice * s->dims.nx) * p->inc_iline) * p->iline_distance);
+    a.adx = (float)(p->inc_iline * p->iline_distance);
+    a.ay0 = (float)((p->start_xline + (s->yslice * s->dims.ny) * p->inc_xline) * p->xline_distance);
+    a.ady = (float)(p->inc_xline * p->xline_distance);
+    if (a.adx == 0.0f) a.adx = 1.0f;
+    if (a.ady == 0.0f) a.ady = 1.0f;
+    a.aperture = p->aperture;
+    a.tmax = (float)ns - 1.0f;
+    a.lmaxf = (float)s->lmax;
+    const float rdt = 1.0f / p->dt;
+    a.rdt2 = rdt * rdt;
+    a.aax = (float)p->iline_distance;
+    a.aay = (float)p->xline_distance;
+    const size_t smem = sizeof(float) * 8 * (size_t)((ns + 3) & ~3);
+    if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
+    KP_CUDA(cudaFuncSetAttribute(k_demig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_demig<<<(unsigned)((c->lsm_nlive + 7) / 8), 256, smem, c->cs>>>(a);
+    KP_CUDA(cudaGetLastError());
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t ntr)
+{
+    if (!c || !hdr_be || ntr <= 0 || ntr > INT32_MAX / 2) return KPSTM_ERR_INVALID_ARG;
+    if (c->p.mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED;
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    void *old[] = {c->d_lgraw, c->d_lgeom, c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive,
+                   c->d_lcnt, c->d_ltable, c->d_lkm, c->d_lhits, c->d_dotpart, c->d_dot};
+    for (size_t i = 0; i < sizeof(old) / sizeof(old[0]); ++i)
+        if (old[i]) cudaFree(old[i]);
+    c->d_lgraw = c->d_lgeom = nullptr;
+    c->d_lcls = c->d_lorder = c->d_lcstart = c->d_lnlive = c->d_lcnt = nullptr;
+    c->d_ltable = c->d_lkm = nullptr;
+    c->d_lhits = nullptr;
+    c->d_dotpart = c->d_dot = nullptr;
+    c->lsm_ntr = c->lsm_nlive = 0;
+    const int ns = c->p.ns, ncls = c->s.nclass, tm = c->s.dims.trange_max;
+    const size_t nimg = (size_t)ncls * c->s.ncol * ns;
+    int32_t *d_hdr = nullptr;
+    KP_CUDA(cudaMalloc(&d_hdr, sizeof(int32_t) * 60 * ntr));
+    int st = KPSTM_OK;
+    do {
+#define KP_LALLOC(ptr, bytes)                                                                                \
+    if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) {                                                        \
+        st = KPSTM_ERR_OUT_OF_MEMORY;                                                                        \
+        break;                                                                                               \
+    }
+        KP_LALLOC(c->d_lgraw, sizeof(kpstm_geom) * ntr);
+        KP_LALLOC(c->d_lgeom, sizeof(kpstm_geom) * ntr);
+        KP_LALLOC(c->d_lcls, sizeof(int32_t) * ntr);
+        KP_LALLOC(c->d_lorder, sizeof(int32_t) * ntr);
+        KP_LALLOC(c->d_lcstart, sizeof(int32_t) * (ncls + 1));
+        KP_LALLOC(c->d_lnlive, sizeof(int32_t));
+        KP_LALLOC(c->d_lkm, sizeof(float) * nimg);
+        KP_LALLOC(c->d_lcnt, sizeof(int32_t) * nimg);
+        KP_LALLOC(c->d_lhits, sizeof(unsigned long long));
+        KP_LALLOC(c->d_dotpart, sizeof(double) * KP_DOT_BLOCKS);
+        KP_LALLOC(c->d_dot, sizeof(double) * 4);
+#undef KP_LALLOC
+        if (cudaMemcpyAsync(d_hdr, hdr_be, sizeof(int32_t) * 60 * ntr, cudaMemcpyHostToDevice, c->cs) !=
+            cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        KpGeomArgs g;
+        memset(&g, 0, sizeof(g));
+        g.hdr_be = d_hdr;
+        g.ntr = ntr;
+        g.geom = c->d_lgraw;
+        g.cls = c->d_lcls;
+        g.status = c->d_status;
+        g.ox = c->p.ox;
+        g.oy = c->p.oy;
+        g.xy_scale = c->p.xy_scale;
+        g.oh = c->p.oh;
+        g.dh = c->p.dh;
+        g.cull_radius = c->s.cull_radius;
+        g.sinA = c->s.sinA;
+        g.cosA = c->s.cosA;
+        g.IXc = c->s.IXc;
+        g.IYc = c->s.IYc;
+        g.nh = c->p.nh;
+        g.stack = c->p.output == KPSTM_OUT_STACK;
+        k_geometry<<<(unsigned)((ntr + 255) / 256), 256, 0, c->cs>>>(g);
+        k_bucket<<<1, 1024, sizeof(int32_t) * (ncls + 1), c->cs>>>(c->d_lcls, ntr, ncls, c->d_lcstart,
+                                                                      c->d_lorder, c->d_lnlive);
+        k_gather_geom<<<(unsigned)((ntr + 255) / 256), 256, 0, c->cs>>>(c->d_lgraw, c->d_lorder, c->d_lnlive,
+                                                                        c->d_lgeom);
+        int32_t nl = 0;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(&nl, c->d_lnlive, sizeof(int32_t), cudaMemcpyDeviceToHost, c->cs) != cudaSuccess ||
+            cudaStreamSynchronize(c->cs) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        c->lsm_ntr = ntr;
+        c->lsm_nlive = nl;
+        c->lrow = ((4 * (int64_t)(ns + 2 * tm - 3)) + 3) & ~int64_t(3);
+        if (cudaMalloc(&c->d_ltable, sizeof(float) * c->lrow * (size_t)(nl > 0 ? nl : 1)) != cudaSuccess) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+    } while (0);
+    cudaFree(d_hdr);
+    if (st) return st;
+    return check_status(c);
+}
+
+extern "C" int kpstm_lsm_adjoint(kpstm_ctx *c, const float *d_data, float *d_model)
+{
+    if (!c || !d_data || !d_model) return KPSTM_ERR_INVALID_ARG;
+    if (!c->d_lgeom) return KPSTM_ERR_STATE;
+    int st = lsm_adjoint_impl(c, d_data, nullptr, nullptr, d_model);
+    if (st) return st;
+    return check_status(c);
+}
+
+extern "C" int kpstm_lsm_forward(kpstm_ctx *c, const float *d_model, float *d_data)
+{
+    if (!c || !d_data || !d_model) return KPSTM_ERR_INVALID_ARG;
+    if (!c->d_lgeom) return KPSTM_ERR_STATE;
+    int st = lsm_forward_impl(c, d_model, d_data);
+    if (st) return st;
+    return check_status(c);
+}
+
+static int dot(kpstm_ctx *c, const float *x, const float *y, int64_t n, double *out)
+{
+    k_dot_partial<<<KP_DOT_BLOCKS, 256, 0, c->cs>>>(x, y, n, c->d_dotpart);
+    k_dot_final<<<1, 256, 0, c->cs>>>(c->d_dotpart, KP_DOT_BLOCKS, c->d_dot);
+    KP_CUDA(cudaGetLastError());
+    KP_CUDA(cudaMemcpyAsync(out, c->d_dot, sizeof(double), cudaMemcpyDeviceToHost, c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    return KPSTM_OK;
+}
+
+/* CGLS: r = d - L x, s = L^T r, p = s; q = L p, alpha = |s|^2/|q|^2,
+   x += alpha p, r -= alpha q, s = L^T r, beta = |s_new|^2/|s|^2, p = s + beta p. */
+extern "C" int kpstm_lsm_cg(kpstm_ctx *c, const float *d_data, int32_t niter, float *d_model, double *resid)
+{
+    if (!c || !d_data || !d_model || niter < 0) return KPSTM_ERR_INVALID_ARG;
+    if (!c->d_lgeom) return KPSTM_ERR_STATE;
+    const int ns = c->p.ns;
+    const int64_t nd = c->lsm_ntr * (int64_t)ns, nm = c->s.dims.out_elems;
+    const bool bf16 = c->p.precision == KPSTM_PREC_BF16_KAHAN;
+    float *r = nullptr, *q = nullptr, *sv = nullptr, *pv = nullptr, *scale = nullptr;
+    uint16_t *r16 = nullptr;
+    int st = KPSTM_OK;
+    do {
+        if (cudaMalloc(&r, sizeof(float) * nd) != cudaSuccess || cudaMalloc(&q, sizeof(float) * nd) != cudaSuccess ||
+            cudaMalloc(&sv, sizeof(float) * nm) != cudaSuccess || cudaMalloc(&pv, sizeof(float) * nm) != cudaSuccess) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        if (bf16 && (cudaMalloc(&r16, sizeof(uint16_t) * nd) != cudaSuccess ||
+                     cudaMalloc(&scale, sizeof(float) * c->lsm_ntr) != cudaSuccess)) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        const unsigned tb = (unsigned)((c->lsm_ntr * 32 + 255) / 256);
+        /* x = 0, r = d (stored bf16 when asked) */
+        if (cudaMemsetAsync(d_model, 0, sizeof(float) * nm, c->cs) != cudaSuccess ||
+            cudaMemcpyAsync(r, d_data, sizeof(float) * nd, cudaMemcpyDeviceToDevice, c->cs) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        auto store_r = [&]() -> int {
+            if (!bf16) return KPSTM_OK;
+            k_to_bf16<<<tb, 256, 0, c->cs>>>(r, c->lsm_ntr, ns, r16, scale);
+            k_from_bf16<<<1024, 256, 0, c->cs>>>(r16, scale, c->lsm_ntr, ns, r);
+            KP_CUDA(cudaGetLastError());
+            return KPSTM_OK;
+        };
+        auto adjoint_r = [&](float *out) -> int {
+            return bf16 ? lsm_adjoint_impl(c, nullptr, r16, scale, out) : lsm_adjoint_impl(c, r, nullptr, nullptr, out);
+        };
+        if ((st = store_r())) break;
+        double rr = 0.0;
+        if ((st = dot(c, r, r, nd, &rr))) break;
+        if (resid) resid[0] = sqrt(rr);
+        if ((st = adjoint_r(sv))) break;
+        if (cudaMemcpyAsync(pv, sv, sizeof(float) * nm, cudaMemcpyDeviceToDevice, c->cs) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        double gamma = 0.0;
+        if ((st = dot(c, sv, sv, nm, &gamma))) break;
+        for (int it = 0; it < niter; ++it) {
+            if ((st = lsm_forward_impl(c, pv, q))) break;
+            double qq = 0.0;
+            if ((st = dot(c, q, q, nd, &qq))) break;
+            const double alpha = qq > 0.0 ? gamma / qq : 0.0;
+            k_axpby<<<1024, 256, 0, c->cs>>>(d_model, pv, (float)alpha, 1.0f, nm);
+            k_axpby<<<1024, 256, 0, c->cs>>>(r, q, (float)(-alpha), 1.0f, nd);
+            if ((st = store_r())) break;
+            if (resid) {
+                if ((st = dot(c, r, r, nd, &rr))) break;
+                resid[it + 1] = sqrt(rr);
+            }
+            if ((st = adjoint_r(sv))) break;
+            double gnew = 0.0;
+            if ((st = dot(c, sv, sv, nm, &gnew))) break;
+            const double beta = gamma > 0.0 ? gnew / gamma : 0.0;
+            gamma = gnew;
+            k_axpby<<<1024, 256, 0, c->cs>>>(pv, sv, 1.0f, (float)beta, nm);
+            if (cudaGetLastError() != cudaSuccess) {
+                st = KPSTM_ERR_CUDA;
+                break;
+            }
+        }
+    } while (0);
+    cudaStreamSynchronize(c->cs);
+    cudaFree(r);
+    cudaFree(q);
+    cudaFree(sv);
+    cudaFree(pv);
+    cudaFree(r16);
+    cudaFree(scale);
+    if (st) return st;
+    return check_status(c);
 }

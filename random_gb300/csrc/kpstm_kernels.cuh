@@ -46,7 +46,7 @@ struct KpPrepArgs {
     const double *c4;              /* [ns] 4*t2[t] */
     const double *c4r;             /* [ns] RN(1/(4*t2[t])) */
     int64_t row;                   /* floats per table row */
-    int ns, tm, full;
+    int ns, tm, full, hilo;        /* hilo: full-mode rows of float4 {hi, lo, dP, 0} */
     float dt;
 };
 
@@ -219,7 +219,11 @@ __global__ void k_prep(KpPrepArgs a)
 #define KP_SAMPLE(t) (f32 ? f32[(t)] : __fmul_rn(__uint_as_float(((uint32_t)f16[(t)]) << 16), sc))
     if (a.full) {
         float2 *q = reinterpret_cast<float2 *>(row); /* q[i + tm] for P index i */
-        for (int j = tm; j > 1; --j) q[tm - j] = make_float2(0.0f, 0.0f);
+        float4 *q4 = reinterpret_cast<float4 *>(row);
+        for (int j = tm; j > 1; --j) {
+            if (a.hilo) q4[tm - j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            else q[tm - j] = make_float2(0.0f, 0.0f);
+        }
         double p1 = 0.0, p2 = 0.0;
         /* last P index stored: the imaging kernel reads entry floor(x) + tm with
            x < ns - 2 + lmax and lmax <= tm - 1, i.e. entries 0 .. ns + 2tm - 4 */
@@ -228,7 +232,12 @@ __global__ void k_prep(KpPrepArgs a)
             if (t < ns) p1 += (double)KP_SAMPLE(t);
             const double prev = p2;
             p2 += p1; /* P[t] */
-            q[t - 1 + tm] = make_float2((float)prev, (float)p1); /* entry of P index t-1 */
+            if (a.hilo) {
+                const float hi = (float)prev;
+                q4[t - 1 + tm] = make_float4(hi, (float)(prev - (double)hi), (float)p1, 0.0f);
+            } else {
+                q[t - 1 + tm] = make_float2((float)prev, (float)p1); /* entry of P index t-1 */
+            }
         }
         return;
     }
@@ -263,6 +272,35 @@ __global__ void k_prep(KpPrepArgs a)
 }
 
 /* ------------------------------------------------------------------------ */
+/* Full-mode pair arithmetic shared by the migration (k_image) and its
+   adjoint (k_demig), so that both see bit-identical pair sets, traveltimes,
+   triangle widths and weights.  Sample units: tv = {(t/2)^2, 1/(v dt)^2},
+   dIS2/dIR2 the squared image-source/receiver distances, a* the distance
+   components times the line spacings. */
+struct KpPair {
+    float Tf;  /* traveltime in samples */
+    float Lf;  /* triangle half-width in samples, 1..lmax */
+    float w;   /* (1/ts' + 1/tr')^2 / Lf^2; the factor t/(8 dt) is applied outside */
+};
+
+__device__ __forceinline__ float kp_pair_time(float dIS2, float dIR2, float2 tv, float &rs, float &rr)
+{
+    const float as = __fmaf_rn(dIS2, tv.y, tv.x), ar = __fmaf_rn(dIR2, tv.y, tv.x);
+    rs = kp_rsqrt_approx(as);
+    rr = kp_rsqrt_approx(ar);
+    return __fmaf_rn(as, rs, __fmul_rn(ar, rr));
+}
+
+__device__ __forceinline__ void kp_pair_width(float rs, float rr, float axs, float axr, float ays, float ayr,
+                                              float rv2, float lmaxf, float &Lf, float &w)
+{
+    const float gxx = __fmaf_rn(axs, rs, __fmul_rn(axr, rr)), gyy = __fmaf_rn(ays, rs, __fmul_rn(ayr, rr));
+    Lf = fminf(__fmaf_rn(__fadd_rn(fabsf(gxx), fabsf(gyy)), rv2, 1.0f), lmaxf);
+    const float ui = __fmul_rn(__fadd_rn(rs, rr), kp_rcp_approx(Lf));
+    w = __fmul_rn(ui, ui);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Imaging.  Grid (ntile, ncls, nwin); block 256 = 8 warps; warp w owns image
    column blockIdx.x*8 + w, lane l owns samples tw0 + l + 32k, k < K. */
 
@@ -273,7 +311,7 @@ __device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float 
     return dx * dx + dy * dy < r2;
 }
 
-template <int K, bool FULL, bool KAHAN>
+template <int K, bool FULL, bool KAHAN, bool HILO = false>
 __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
 {
     constexpr int W = 32 * K;
@@ -482,38 +520,48 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
                            accumulators are read (ts' = ts/dt) */
                         const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
                         const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
-                        /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm */
+                        /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm;
+                           the hi/lo table {hi(P(i)), lo(P(i)), P(i+1)-P(i), 0} keeps P to
+                           ~1e-14 for noisy traces (least-squares operators) */
                         const float2 *q2 = reinterpret_cast<const float2 *>(tab) + a.tm;
+                        const float4 *q4 = reinterpret_cast<const float4 *>(tab) + a.tm;
 #pragma unroll
                         for (int k = 0; k < K; ++k) {
                             const float2 tv = sv[32 * k]; /* sample tw0 + lane + 32k */
-                            const float as = fmaf(dIS2, tv.y, tv.x), ar = fmaf(dIR2, tv.y, tv.x);
-                            const float rs = kp_rsqrt_approx(as), rr = kp_rsqrt_approx(ar);
-                            const float Tf = fmaf(as, rs, ar * rr);
+                            float rs, rr;
+                            const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
                             if (Tf < tmax) { /* late samples of far traces skip the taps (whole warps) */
-                                const float gxx = fmaf(axs, rs, axr * rr), gyy = fmaf(ays, rs, ayr * rr);
-                                const float Lf = fminf(fmaf(fabsf(gxx) + fabsf(gyy), tv.y, 1.0f), a.lmaxf);
+                                float Lf, wgt;
+                                kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
                                 const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
                                 const int b0 = kp_floor_bits(x0), ba = kp_floor_bits(xa), bb = kp_floor_bits(xb);
                                 const float f0 = x0 - (__int_as_float(b0) - KP_MAGIC);
                                 const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
                                 const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
-                                const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
-                                const float2 Qb = q2[bb - KP_MAGIC_BITS];
                                 /* second difference without cancellation: table differences
-                                   (exact for neighbouring values) plus the interpolation terms */
-                                const float big = (Qa.x - Q0.x) + (Qb.x - Q0.x);
-                                const float small = fmaf(fa, Qa.y, fb * Qb.y) - 2.0f * (f0 * Q0.y);
-                                const float ui = (rs + rr) * kp_rcp_approx(Lf);
+                                   (exact for neighbouring values) plus the interpolation terms;
+                                   equals sum_k f[k] max(0, Lf - |Tf - k|) */
+                                float big, small;
+                                if (HILO) {
+                                    const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
+                                    const float4 Qb = q4[bb - KP_MAGIC_BITS];
+                                    big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
+                                    small = fmaf(fa, Qa.z, fb * Qb.z) - 2.0f * (f0 * Q0.z);
+                                } else {
+                                    const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
+                                    const float2 Qb = q2[bb - KP_MAGIC_BITS];
+                                    big = (Qa.x - Q0.x) + (Qb.x - Q0.x);
+                                    small = fmaf(fa, Qa.y, fb * Qb.y) - 2.0f * (f0 * Q0.y);
+                                }
                                 float &ak = (k & 1) ? acc[k >> 1].y : acc[k >> 1].x;
                                 if (KAHAN) {
                                     float &ck = (k & 1) ? comp[k >> 1].y : comp[k >> 1].x;
-                                    float y = fmaf(ui * ui, big + small, -ck);
+                                    float y = fmaf(wgt, big + small, -ck);
                                     float s = ak + y;
                                     ck = (s - ak) - y;
                                     ak = s;
                                 } else {
-                                    ak = fmaf(ui * ui, big + small, ak);
+                                    ak = fmaf(wgt, big + small, ak);
                                 }
                                 cnt[k] += 1;
                             }
@@ -546,6 +594,179 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
         }
     }
     if (blockIdx.z == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Least-squares migration: the adjoint of the full-mode migration
+   (demigration, data = L model) and vector kernels for conjugate gradients. */
+
+struct KpDemigArgs {
+    const kpstm_geom *geom;        /* live traces, slot order; geom.cls = class */
+    const int32_t *nlive;
+    const float *model;            /* [ncol][ncls][ns] */
+    const float *tscale;           /* [ns] t / (8 dt) */
+    const float2 *colxy;
+    const int32_t *colrow;
+    const float2 *vrows;           /* [nrow][ns] {v^2, RN(1/v^2)} */
+    const float2 *t2c;             /* [ns] {(t/2)^2, .} */
+    float *out;                    /* [ntr][ns] in block order */
+    int *status;
+    int nx, ny, ncls, ns;
+    float ax0, adx, ay0, ady;      /* column coordinates: IX(xc) ~ ax0 + xc adx */
+    double aperture;
+    float tmax, lmaxf, rdt2, aax, aay;
+};
+
+/* One warp per live trace: visits the image columns within the aperture of
+   the trace's midpoint (the same exact float test as k_image), computes every
+   pair with the same routines as k_image, and scatters
+   W max(0, Lf - |Tf - k|) into the trace (shared memory), W = weight x
+   t/(8 dt) x model - the exact transpose of k_image's
+   sum_k f[k] max(0, Lf - |Tf - k|). */
+__global__ void __launch_bounds__(256) k_demig(KpDemigArgs a)
+{
+    extern __shared__ float dm_acc[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ns = a.ns;
+    const int nsp = (ns + 3) & ~3;
+    float *acc = dm_acc + w * nsp;
+    for (int k = lane; k < nsp; k += 32) acc[k] = 0.0f;
+    __syncwarp();
+    const int slot = blockIdx.x * 8 + w;
+    if (slot >= *a.nlive) return; /* warps are independent: no block barrier below */
+    const kpstm_geom g = a.geom[slot];
+    const int cls = g.cls;
+    const float apm = (float)a.aperture * 1.00001f + 1.0f; /* range margin; exact test below */
+    const int x_lo = max(0, (int)floorf((g.cmpx - apm - a.ax0) / a.adx) - 1);
+    const int x_hi = min(a.nx - 1, (int)ceilf((g.cmpx + apm - a.ax0) / a.adx) + 1);
+    for (int xc = x_lo; xc <= x_hi; ++xc) {
+        const float dxc = fmaf((float)xc, a.adx, a.ax0) - g.cmpx;
+        const float rem = apm * apm - dxc * dxc;
+        if (rem < 0.0f) continue;
+        const float dyr = sqrtf(rem) + 1.0f;
+        const int y_lo = max(0, (int)floorf((g.cmpy - dyr - a.ay0) / a.ady) - 1);
+        const int y_hi = min(a.ny - 1, (int)ceilf((g.cmpy + dyr - a.ay0) / a.ady) + 1);
+        for (int yc = y_lo; yc <= y_hi; ++yc) {
+            const int col = xc * a.ny + yc;
+            const float2 cxy = a.colxy[col];
+            const float IX = cxy.x, IY = cxy.y;
+            float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
+            float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
+            if (!((double)dIC < a.aperture)) continue;
+            const int vrow = a.colrow[col];
+            if (vrow < 0) {
+                kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
+                continue;
+            }
+            float sx = __fsub_rn(IX, g.sxt), sy = __fsub_rn(IY, g.syt);
+            float gx = __fsub_rn(IX, g.gxt), gy = __fsub_rn(IY, g.gyt);
+            const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
+            const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
+            const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
+            const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
+            const float *m = a.model + ((int64_t)col * a.ncls + cls) * ns;
+            const float2 *vr = a.vrows + (int64_t)vrow * ns;
+            for (int t0 = 0; t0 < ns; t0 += 32) {
+                const int t = t0 + lane;
+                if (t >= ns) continue;
+                const float mv = m[t];
+                if (mv == 0.0f) continue;
+                const float2 tv = make_float2(a.t2c[t].x, vr[t].y * a.rdt2);
+                float rs, rr;
+                const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
+                if (!(Tf < a.tmax)) continue;
+                float Lf, wgt;
+                kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
+                const float W = wgt * (a.tscale[t] * mv);
+                const int k0 = max(0, (int)floorf(Tf - Lf) + 1);
+                const int k1 = min(ns - 1, (int)ceilf(Tf + Lf) - 1);
+                for (int k = k0; k <= k1; ++k) {
+                    const float wk = Lf - fabsf(Tf - (float)k);
+                    if (wk > 0.0f) atomicAdd(&acc[k], W * wk);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    float *o = a.out + (int64_t)g.src * ns;
+    for (int k = lane; k < ns; k += 32) o[k] = acc[k];
+}
+
+/* live slot -> geometry in slot order */
+__global__ void k_gather_geom(const kpstm_geom *graw, const int32_t *order, const int32_t *nlive, kpstm_geom *geom)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *nlive) geom[i] = graw[order[i]];
+}
+
+/* Deterministic FP64 dot product: per-block partial sums, then one block. */
+#define KP_DOT_BLOCKS 1024
+__global__ void __launch_bounds__(256) k_dot_partial(const float *x, const float *y, int64_t n, double *part)
+{
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)x[i] * (double)y[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) k_dot_final(const double *part, int nparts, double *out)
+{
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+/* y = a*x + b*y (a, b from the host, FP64 scalars rounded once to float) */
+__global__ void k_axpby(float *y, const float *x, float av, float bv, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = fmaf(av, x[i], bv * y[i]);
+}
+
+/* fp32 traces -> bf16 with a per-trace scale (max |x| / 256, a power of two
+   so that decode is exact); one warp per trace. */
+__global__ void k_to_bf16(const float *x, int64_t ntr, int ns, uint16_t *out, float *scale)
+{
+    const int64_t tr = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (tr >= ntr) return;
+    const float *xr = x + tr * ns;
+    float mx = 0.0f;
+    for (int k = lane; k < ns; k += 32) mx = fmaxf(mx, fabsf(xr[k]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    /* scale = 2^e with max|x|/scale in [128, 256): bf16 keeps 8 significant bits */
+    float sc = 1.0f;
+    if (mx > 1e-30f) sc = exp2f(floorf(log2f(mx)) - 7.0f); /* zero or denormal traces keep scale 1 */
+    const float inv = 1.0f / sc;
+    uint16_t *o = out + tr * ns;
+    for (int k = lane; k < ns; k += 32) {
+        const float v = xr[k] * inv;
+        const uint32_t u = __float_as_uint(v);
+        o[k] = (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16); /* round to nearest even */
+    }
+    if (lane == 0) scale[tr] = sc;
+}
+
+/* bf16 traces (with per-trace scale) -> fp32 */
+__global__ void k_from_bf16(const uint16_t *in, const float *scale, int64_t ntr, int ns, float *x)
+{
+    const int64_t n = ntr * ns;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = __uint_as_float(((uint32_t)in[i]) << 16) * scale[i / ns];
 }
 
 /* ------------------------------------------------------------------------ */

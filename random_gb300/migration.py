@@ -112,6 +112,24 @@ class Migration:
         capi.check("kpstm_profile_read", self._lib.kpstm_profile_read(self._h, C.byref(pr)))
         return {f: getattr(pr, f) for f, _ in capi.KpstmProfile._fields_}
 
+    # -- least-squares migration (device pointers) ----------------------------
+    def lsm_geometry(self, headers: np.ndarray, headers_are_be: bool = False) -> None:
+        hdr = np.ascontiguousarray(headers if headers_are_be else segy.headers_be(headers), dtype=np.int32)
+        capi.check("kpstm_lsm_geometry", self._lib.kpstm_lsm_geometry(self._h, hdr.ctypes.data, hdr.shape[0]))
+
+    def lsm_adjoint(self, d_data: int, d_model: int) -> None:
+        """d_model = L^T d_data (migration)."""
+        capi.check("kpstm_lsm_adjoint", self._lib.kpstm_lsm_adjoint(self._h, d_data, d_model))
+
+    def lsm_forward(self, d_model: int, d_data: int) -> None:
+        """d_data = L d_model (demigration)."""
+        capi.check("kpstm_lsm_forward", self._lib.kpstm_lsm_forward(self._h, d_model, d_data))
+
+    def lsm_cg(self, d_data: int, niter: int, d_model: int) -> np.ndarray:
+        resid = np.zeros(niter + 1, np.float64)
+        capi.check("kpstm_lsm_cg", self._lib.kpstm_lsm_cg(self._h, d_data, niter, d_model, resid.ctypes.data))
+        return resid
+
     def synchronize(self) -> None:
         capi.check("kpstm_synchronize", self._lib.kpstm_synchronize(self._h))
 
