@@ -103,11 +103,12 @@ class ClockSampler:
 
 # ----------------------------------------------------------------- workload
 def survey_model(rank: int = 0, ntr: int = SURVEY_TRACES):
-    from random_gb300 import synth
+    from random_gb300 import multirank, synth
     # each rank: its own 10 km x 10 km slab (x shifted), same statistics
     return synth.patch3d_model(ntr, ns=NS, dt=DT, nx=NX, ny=NY, bin_m=25.0, max_offset=4000.0,
                                n_refl=8, n_diff=200, freq=30.0, aperture=3000.0, aa_cutoff=100.0,
-                               seed=2 + rank, mode=1, output=1, x_shift=rank * 20000.0)
+                               seed=2 + rank, mode=1, output=1,
+                               x_shift=multirank.weak_scaling_shift(rank, 20000.0))
 
 
 def algorithmic_bytes_per_step(model, ntr_step: int, row_floats: int) -> int:
@@ -179,7 +180,7 @@ def host_cores() -> int:
 def run_ours(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
-    from random_gb300 import build, capi, segy, synth
+    from random_gb300 import build, capi, multirank, segy, synth
     from random_gb300.migration import Migration
 
     build.build()
@@ -231,21 +232,13 @@ def run_ours(args, rank, world, local_rank):
     prof = m.profile_read()
     m.profile(False)
     pairs = m.pairs() - pairs0
-    tot = torch.tensor([elapsed, float(pairs)], dtype=torch.float64, device=dev)
-    if world > 1:
-        mx = tot[:1].clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm_ = tot[1:].clone()
-        dist.all_reduce(sm_, op=dist.ReduceOp.SUM)
-        elapsed_max, pairs_all = float(mx.item()), float(sm_.item())
-    else:
-        elapsed_max, pairs_all = elapsed, float(pairs)
+    elapsed_max, pairs_all = multirank.reduce_timing(elapsed, float(pairs), device=dev)
     value = pairs_all / elapsed_max / 1e9
 
     # roofline of the imaging kernel (dominant: see profile shares)
     launches = max(1, int(prof["image_launches"]))
     t_launch = prof["image_ms"] / 1e3 / launches
-    row_floats = 2 * (NS + 2 * m.dims["trange_max"] - 3)
+    row_floats = 2 * (NS + 2 * m.dims["trange_max"] - 2)
     row_floats = (row_floats + 3) & ~3
     b_alg = algorithmic_bytes_per_step(model, block, row_floats)
     achieved = b_alg / t_launch / 1e9
@@ -316,6 +309,123 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------- further workloads (not the bench line)
+def _timed_steps(step, warmup, steps, stream):
+    import torch
+    for i in range(warmup):
+        step(i)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        step(warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, clocks.stop()
+
+
+def run_offset_bins(args):
+    """64 offset bins over 0-4000 m, Poisson(15000) traces per bin clipped to
+    [2000, 40000] (960,790 traces), ns = 1001 at 4 ms, each bin imaged into
+    160 x 160 x 1001 offset gathers, reference operator with BF16 trace
+    storage and Kahan accumulation; the launch configuration is autotuned on
+    the first 8,000 traces, then each block is imaged by one persistent launch
+    replayed from a CUDA graph.  A step is a block of traces of all bins."""
+    import torch
+    from random_gb300 import build, capi, segy, synth
+    from random_gb300.migration import Migration
+    build.build()
+    dev = torch.device("cuda", 0)
+    counts = synth.offset_bin_counts(64, 15000.0, 2000, 40000, seed=4)
+    mdl = synth.offset_bins_model(counts, ns=1001, dt=0.004, nx=160, ny=160, bin_m=12.5, aperture=1500.0,
+                                  n_refl=8, n_diff=200, freq=25.0, mode=capi.MODE_REFERENCE, aa_cutoff=1e6)
+    s = mdl.survey
+    d_hdr = torch.from_numpy(np.ascontiguousarray(segy.headers_be(s.headers))).to(dev)
+    d_smp = synth.synthesize_torch(mdl, device=dev)
+    torch.cuda.synchronize()
+    block = args.traces_per_step if args.traces_per_step != STEP_TRACES else 120_000
+    nblocks = s.ntr // block
+    m = Migration(dict(s.params, precision=capi.PREC_BF16_KAHAN), s.velocity)
+    stream = torch.cuda.Stream(device=dev)
+    m.set_stream(stream.cuda_stream)
+    m.set_launch(persistent=1, graph=1)
+    cfg, tune_ms = m.autotune(d_hdr.data_ptr(), d_smp.data_ptr(), 8000)
+    m.set_launch(**dict(cfg, persistent=1, graph=1))
+    row = 1001 * 4
+
+    def step(i):
+        b = i % nblocks
+        m.add_traces_device(d_hdr.data_ptr() + b * block * 240, d_smp.data_ptr() + b * block * row, block)
+
+    p0 = m.pairs()
+    elapsed, clk = _timed_steps(step, args.warmup, args.steps, stream)
+    m.synchronize()
+    pairs = m.pairs() - p0
+    pairs_timed = pairs * args.steps / (args.steps + args.warmup)
+    line = {"workload": "offset-bins", "metric": METRIC, "value": round(pairs_timed / elapsed / 1e9, 4),
+            "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(elapsed / args.steps * 1e3, 3), "dtype": "bf16 store, f32 compute",
+            "config": {"bins": 64, "traces": int(s.ntr), "traces_per_step": block, "ns": 1001,
+                       "image": "160x160x64x1001", "launch": cfg, "autotune_ms": round(tune_ms, 3)},
+            "pairs_per_step_est": pairs / (args.steps + args.warmup), "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_lsm(args):
+    """Least-squares operator pair on 250,000 traces (ns = 751 at 4 ms,
+    offsets U(0, 3000 m), random azimuths) and a 200 x 200 x 751 model at
+    25 m, aperture 3000 m, full physics: a step is one demigration d = L m
+    plus one migration L^T d (the work of one CG iteration), BF16 data."""
+    import torch
+    from random_gb300 import build, capi, synth
+    from random_gb300.migration import Migration
+    build.build()
+    dev = torch.device("cuda", 0)
+    ntr = args.survey_traces if args.survey_traces != SURVEY_TRACES else 250_000
+    mdl = synth.patch3d_model(ntr, ns=751, dt=0.004, nx=200, ny=200, bin_m=25.0, max_offset=3000.0, n_refl=12,
+                              n_diff=100, freq=25.0, aperture=3000.0, seed=5, mode=capi.MODE_FULL,
+                              output=capi.OUT_STACK)
+    s = mdl.survey
+    m = Migration(dict(s.params, precision=capi.PREC_BF16_KAHAN), s.velocity)
+    stream = torch.cuda.Stream(device=dev)
+    m.set_stream(stream.cuda_stream)
+    m.lsm_geometry(s.headers)
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    model = torch.randn(*m.shape, device=dev, generator=g)
+    data = torch.empty((ntr, 751), device=dev)
+    torch.cuda.synchronize()
+    t = {"fwd": 0.0, "adj": 0.0}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def step(i):
+        ev[0].record(stream)
+        m.lsm_forward(model.data_ptr(), data.data_ptr())
+        ev[1].record(stream)
+        m.lsm_adjoint(data.data_ptr(), model.data_ptr())
+        ev[2].record(stream)
+        model.mul_(1.0 / (model.abs().max() + 1e-30))  # keep magnitudes bounded between steps
+        if i >= args.warmup:
+            torch.cuda.synchronize()
+            t["fwd"] += ev[0].elapsed_time(ev[1]) / 1e3
+            t["adj"] += ev[1].elapsed_time(ev[2]) / 1e3
+
+    with torch.cuda.stream(stream):
+        elapsed, clk = _timed_steps(step, args.warmup, args.steps, stream)
+    pairs_app = m.lsm_pairs()
+    line = {"workload": "lsm-operator-pair", "metric": METRIC,
+            "value": round(2 * pairs_app * args.steps / (t["fwd"] + t["adj"]) / 1e9, 4), "unit": UNIT,
+            "steps": args.steps, "warmup": args.warmup, "dtype": "bf16 data, f32 compute",
+            "forward_gpairs_s": round(pairs_app * args.steps / t["fwd"] / 1e9, 4),
+            "adjoint_gpairs_s": round(pairs_app * args.steps / t["adj"] / 1e9, 4),
+            "pairs_per_application": pairs_app,
+            "config": {"traces": ntr, "ns": 751, "model": "200x200x751", "aperture_m": 3000.0},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -357,12 +467,20 @@ def main():
     ap.add_argument("--ref-traces", type=int, default=1500)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["survey", "offset-bins", "lsm"], default="survey",
+                    help="survey: the bench line; offset-bins / lsm: further measurements (1 GPU)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "offset-bins":
+        run_offset_bins(args)
+        return
+    if args.workload == "lsm":
+        run_lsm(args)
         return
     if world > 1:
         import torch

@@ -201,6 +201,41 @@ typedef struct {
 int kpstm_profile_enable(kpstm_ctx *ctx, int enable);
 int kpstm_profile_read(kpstm_ctx *ctx, kpstm_profile *out);
 
+/* ---- launch configuration of the imaging kernel ----------------------------- */
+/* No counterpart in the reference (its loop order is fixed: trace, column,
+   sample, Kirchhoff.c:1292-1403).  A work item of the imaging kernel is one
+   image tile (8 columns: a tile_px x tile_py patch, one column per warp) x one
+   offset class x one time window of 32*samples_per_lane samples.  None of the
+   choices changes a result: every column still sums its traces in block
+   order, so all configurations give bit-identical images. */
+typedef struct {
+    int tile_px;          /* patch columns along the inline axis: 1, 2, 4 or 8
+                             (tile_py = 8 / tile_px); 0 = default */
+    int samples_per_lane; /* 8, 16, 24 or 32 (full mode <= 24, BF16/Kahan <= 16);
+                             0 = default (the fewest windows, then the smallest K) */
+    int persistent;       /* 1: one resident grid takes (class, tile, window) items
+                             from a device counter, largest classes first;
+                             0: one CTA per item */
+    int graph;            /* 1: each block's device pipeline (geometry, bucketing,
+                             tap tables, imaging) is captured once per block shape
+                             into a CUDA graph and replayed; ignored while
+                             profiling is enabled */
+    int reserved[4];
+} kpstm_launch;
+int kpstm_get_launch(const kpstm_ctx *ctx, kpstm_launch *cfg);
+/* KPSTM_ERR_INVALID_ARG for a value outside the lists above. */
+int kpstm_set_launch(kpstm_ctx *ctx, const kpstm_launch *cfg);
+/* Autotuner: images the given device block (the layout of
+   kpstm_add_traces_device) once per candidate configuration (tile_px x
+   samples_per_lane x persistent; the caller's graph flag is kept), times the
+   imaging kernel with CUDA events, selects the fastest, clears the image
+   accumulators again and returns the choice in *best (nullable) and its time
+   in *best_ms (nullable).  Only on a context without traces since
+   kpstm_create / kpstm_reset (else KPSTM_ERR_STATE).  A few thousand traces
+   of the job's own data are a representative sample. */
+int kpstm_autotune(kpstm_ctx *ctx, const int32_t *d_hdr_be, const float *d_samples, int64_t ntr,
+                   kpstm_launch *best, float *best_ms);
+
 /* ---- least-squares migration ------------------------------------------------ */
 /* No counterpart in the reference.  The operator pair is the full-physics
    migration without its finishing: L^T (migration) maps data d[ntr][ns] to

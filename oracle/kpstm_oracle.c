@@ -510,3 +510,221 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
     free(t1);
     return st;
 }
+
+/* ------------------------------------------------------------------------ */
+/* FP64 oracle. */
+typedef struct {
+    double sxt, syt, gxt, gyt, cx, cy;
+    int off, live;
+} ko_geom64;
+
+typedef struct {
+    const kpstm_params *p;
+    const kpstm_velocity *v;
+    const ko_dims *d;
+    const ko_geom64 *geom;
+    const double *D;       /* reference mode: [ntr][ns] taps */
+    const float *samples;  /* full mode */
+    const double *t2;
+    const int *t1;
+    int64_t ntr;
+    int full, lmax;
+    double *km, *fold;
+    int next_col, err;
+    pthread_mutex_t mu;
+} ko_job64;
+
+static void *column_worker64(void *arg)
+{
+    ko_job64 *J = (ko_job64 *)arg;
+    const kpstm_params *p = J->p;
+    const kpstm_velocity *v = J->v;
+    const ko_dims *d = J->d;
+    const int ns = d->ns, nh = d->nh;
+    const double dt = (double)p->dt;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int col = J->next_col++;
+        pthread_mutex_unlock(&J->mu);
+        if (col >= d->nx * d->ny) break;
+        const int xc = col / d->ny, yc = col % d->ny;
+        const double IX = (p->start_iline + ((xc + d->xslice * d->nx) * p->inc_iline)) * p->iline_distance;
+        const double IY = (p->start_xline + ((yc + d->yslice * d->ny) * p->inc_xline)) * p->xline_distance;
+        int xc1 = (int)round((p->start_iline - v->o_iline) / v->d_iline + (xc + d->xslice * d->nx) * (p->inc_iline / v->d_iline));
+        int yc1 = (int)round((p->start_xline - v->o_xline) / v->d_xline + (yc + d->yslice * d->ny) * (p->inc_xline / v->d_xline));
+        if (xc1 > v->n_iline - 1) xc1 = v->n_iline - 1;
+        if (yc1 > v->n_xline - 1) yc1 = v->n_xline - 1;
+        const int bad = xc1 < 0 || yc1 < 0;
+        const float *vr = bad ? NULL : v->vrms + ((size_t)xc1 * v->n_xline + yc1) * v->nsm;
+        for (int64_t it = 0; it < J->ntr; ++it) {
+            const ko_geom64 *g = &J->geom[it];
+            if (!g->live) continue;
+            if (!(sqrt((IX - g->cx) * (IX - g->cx) + (IY - g->cy) * (IY - g->cy)) < p->aperture)) continue;
+            if (bad) {
+                pthread_mutex_lock(&J->mu);
+                J->err = KPSTM_ERR_VELOCITY_RANGE;
+                pthread_mutex_unlock(&J->mu);
+                break;
+            }
+            const double sx = IX - g->sxt, sy = IY - g->syt, gx = IX - g->gxt, gy = IY - g->gyt;
+            const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
+            double *k = J->km + ((size_t)col * nh + g->off) * ns;
+            double *fo = J->fold + ((size_t)col * nh + g->off) * ns;
+            const double *D = J->D ? J->D + (size_t)it * ns : NULL;
+            const float *f = J->samples + (size_t)it * ns;
+            for (int t = 0; t < ns; ++t) {
+                const double vv = (double)vr[J->t1[t]] * (double)vr[J->t1[t]];
+                if (!J->full) {
+                    const double dsr = sqrt(J->t2[t] + dS2 / vv) + sqrt(J->t2[t] + dR2 / vv);
+                    const double Tq = floor(dsr / dt);
+                    if (Tq < ns) {
+                        k[t] += D[(int)Tq];
+                        fo[t] += 1.0;
+                    }
+                } else {
+                    const double rv2 = 1.0 / vv, t0 = t * dt;
+                    double as = 0.25 * t0 * t0 + dS2 * rv2, ar = 0.25 * t0 * t0 + dR2 * rv2;
+                    if (as < 1e-30) as = 1e-30;
+                    if (ar < 1e-30) ar = 1e-30;
+                    const double ts = sqrt(as), tr = sqrt(ar), T = (ts + tr) / dt;
+                    if (!(T < ns - 1)) continue;
+                    double Lf = 1.0 + fabs((sx / ts + gx / tr) * rv2 * p->iline_distance / dt) +
+                                fabs((sy / ts + gy / tr) * rv2 * p->xline_distance / dt);
+                    if (Lf > J->lmax) Lf = J->lmax;
+                    const double u = 1.0 / ts + 1.0 / tr;
+                    k[t] += t0 / 8.0 * u * u / (Lf * Lf) * full_tri(f, ns, T, Lf);
+                    fo[t] += 1.0;
+                }
+            }
+        }
+    }
+    return NULL;
+}
+
+int ko_kirchhoff64(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be,
+                   const float *samples, int64_t ntr, double *km_out, double *fold_out, double *image)
+{
+    if (!p || !v || (ntr > 0 && (!hdr_be || !samples))) return KPSTM_ERR_INVALID_ARG;
+    ko_dims d;
+    int st = ko_dims_of(p, &d);
+    if (st) return st;
+    const int ns = d.ns, nh = d.nh, full = p->mode == KPSTM_MODE_FULL;
+    int tm;
+    ko_aliasfilter(ns, p->dt, p->iline_distance, p->xline_distance, p->anti_alias_cutoff, &tm, NULL);
+    if (tm < 2) return KPSTM_ERR_TRANGE;
+    int lmax = p->aa_max_halfwidth > 0 ? p->aa_max_halfwidth : tm - 1;
+    if (lmax > tm - 1) lmax = tm - 1;
+    if (lmax > 63) lmax = 63;
+    if (lmax < 1) lmax = 1;
+    const double dt = (double)p->dt;
+    const double cosA = cos(p->angle_e_to_n_deg * KO_PI / 180.0), sinA = sin(p->angle_e_to_n_deg * KO_PI / 180.0);
+    const size_t nimg = (size_t)d.nx * d.ny * nh * ns;
+    double *km = (double *)calloc(nimg, sizeof(double));
+    double *fold = (double *)malloc(sizeof(double) * nimg);
+    double *P = (double *)malloc(sizeof(double) * (ns + 2 * tm));
+    double *D = full ? NULL : (double *)malloc(sizeof(double) * (size_t)(ntr > 0 ? ntr : 1) * ns);
+    double *t2 = (double *)malloc(sizeof(double) * ns);
+    int *t1 = (int *)malloc(sizeof(int) * ns);
+    ko_geom64 *geom = (ko_geom64 *)calloc((size_t)(ntr > 0 ? ntr : 1), sizeof(ko_geom64));
+    if (!km || !fold || !P || (!full && !D) || !t2 || !t1 || !geom) {
+        st = KPSTM_ERR_OUT_OF_MEMORY;
+        goto done64;
+    }
+    for (size_t i = 0; i < nimg; ++i) fold[i] = 1.0;
+    for (int t = 0; t < ns; ++t) {
+        t2[t] = 0.25 * t * t * dt * dt;
+        int q = (int)round((double)t * dt / (double)v->dtm);
+        t1[t] = q > v->nsm - 1 ? v->nsm - 1 : q;
+    }
+    {
+        const double IXc = (p->start_iline + ((d.nx / 2.0 + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance;
+        const double IYc = (p->start_xline + ((d.ny / 2.0 + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance;
+        const double add_on = 0.5 * sqrt(d.nx * p->inc_iline * p->iline_distance * d.nx * p->inc_iline * p->iline_distance +
+                                         d.ny * p->inc_xline * p->xline_distance * d.ny * p->inc_xline * p->xline_distance);
+        for (int64_t it = 0; it < ntr; ++it) {
+            const int32_t *h = hdr_be + (size_t)it * 60;
+            double w4[4];
+            for (int k = 0; k < 4; ++k) w4[k] = (double)be32(h[18 + k]) - (k % 2 == 0 ? p->ox : p->oy);
+            const double si = (double)(int)w4[0], sj = (double)(int)w4[1];
+            const double gi = (double)(int)w4[2], gj = (double)(int)w4[3];
+            ko_geom64 *g = &geom[it];
+            g->sxt = cosA * si + sinA * sj;
+            g->syt = -sinA * si + cosA * sj;
+            g->gxt = cosA * gi + sinA * gj;
+            g->gyt = -sinA * gi + cosA * gj;
+            const double h2 = 0.25 * ((g->sxt - g->gxt) * (g->sxt - g->gxt) + (g->syt - g->gyt) * (g->syt - g->gyt));
+            g->cx = 0.5 * (g->sxt + g->gxt);
+            g->cy = 0.5 * (g->syt + g->gyt);
+            int off = (int)floor((2.0 * sqrt(h2) - p->oh) / p->dh);
+            if (!(off >= 0 && off < p->nh)) continue;
+            g->off = p->output == KPSTM_OUT_STACK ? 0 : off;
+            g->live = sqrt((IXc - g->cx) * (IXc - g->cx) + (IYc - g->cy) * (IYc - g->cy)) < p->aperture + add_on;
+            if (g->live && !full) { /* reference operator in double (Kirchhoff.c:1312-1328, 1391-1392) */
+                const float *f = samples + (size_t)it * ns;
+                P[tm] = f[0];
+                for (int t = 1; t < ns; ++t) P[t + tm] = P[t - 1 + tm] + (double)f[t] / (4.0 * t2[t]);
+                for (int t = ns; t < ns + tm; ++t) P[t + tm] = P[t - 1 + tm] + (double)f[ns - 1] / (dt * dt * t * t);
+                for (int t = 1; t < ns + tm; ++t) P[t + tm] = P[t - 1 + tm] + P[t + tm];
+                for (int t = 0; t < tm; ++t) P[t] = P[2 * tm - t];
+                double *Dt = D + (size_t)it * ns;
+                for (int T = 0; T < ns; ++T) Dt[T] = -2.0 * P[T + tm] + P[T + tm - 2] + P[T + tm + 2];
+            }
+        }
+    }
+    {
+        ko_job64 J;
+        memset(&J, 0, sizeof(J));
+        J.p = p; J.v = v; J.d = &d; J.geom = geom; J.D = D; J.samples = samples; J.t2 = t2; J.t1 = t1;
+        J.ntr = ntr; J.full = full; J.lmax = lmax; J.km = km; J.fold = fold;
+        pthread_mutex_init(&J.mu, NULL);
+        int nthreads = (int)sysconf(_SC_NPROCESSORS_ONLN);
+        if (nthreads < 1) nthreads = 1;
+        if (nthreads > 256) nthreads = 256;
+        pthread_t th[256];
+        int started = 0;
+        for (int k = 0; k < nthreads; ++k)
+            if (pthread_create(&th[k], NULL, column_worker64, &J) == 0) started++;
+        if (started == 0) column_worker64(&J);
+        for (int k = 0; k < started; ++k) pthread_join(th[k], NULL);
+        pthread_mutex_destroy(&J.mu);
+        st = J.err;
+    }
+    if (!st && image) { /* finishing in double (Kirchhoff.c:1457-1479) */
+        double *x = (double *)malloc(sizeof(double) * 2 * ns), *X = (double *)malloc(sizeof(double) * 2 * ns);
+        double *y = (double *)malloc(sizeof(double) * 2 * ns), *aa = (double *)malloc(sizeof(double) * ns);
+        if (!x || !X || !y || !aa) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+        } else {
+            const double fs = 2.0 / dt / ns, fm = 3.0 * p->anti_alias_cutoff;
+            for (int i = 0; i < ns; ++i) aa[i] = 0.0;
+            for (int i = 0; i <= ns / 2; ++i) {
+                const double q = i * fs;
+                aa[i] = 1.0 / sqrt(1.0 + q * q * q * q / (fm * fm * fm * fm));
+            }
+            for (int i = ns / 2; i < ns; ++i) aa[i] = aa[ns - i];
+            for (size_t tr = 0; tr < nimg / ns; ++tr) {
+                const double *kk = km + tr * ns, *ff = fold + tr * ns;
+                x[0] = x[1] = 0.0;
+                for (int t = 1; t < ns; ++t) {
+                    x[2 * t] = -dt * t * (kk[t] - kk[t - 1]) * dt / ff[t];
+                    x[2 * t + 1] = 0.0;
+                }
+                kref_dft(ns, FFTW_FORWARD, x, X);
+                for (int t = 0; t < ns; ++t) {
+                    X[2 * t] *= aa[t];
+                    X[2 * t + 1] *= aa[t];
+                }
+                kref_dft(ns, FFTW_BACKWARD, X, y);
+                double *o = image + tr * ns;
+                o[0] = 0.0;
+                for (int t = 1; t < ns; ++t) o[t] = y[2 * t] / ns;
+            }
+        }
+        free(x); free(X); free(y); free(aa);
+    }
+    if (!st && km_out) memcpy(km_out, km, sizeof(double) * nimg);
+    if (!st && fold_out) memcpy(fold_out, fold, sizeof(double) * nimg);
+done64:
+    free(km); free(fold); free(P); free(D); free(t2); free(t1); free(geom);
+    return st;
+}

@@ -51,6 +51,13 @@ int ko_kirchhoff(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
                  const float *samples, int64_t ntr, float *km, float *fold, float *image,
                  int nthreads, int64_t *pairs);
 
+/* The same job with every quantity in double precision (geometry, running
+   integrals, taps, traveltimes, accumulation, finishing): the FP64 oracle
+   against which the GPU's fp32/bf16 results are measured.  Reference and
+   full modes; outputs [nx][ny][nh][ns] (any may be NULL). */
+int ko_kirchhoff64(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be,
+                   const float *samples, int64_t ntr, double *km, double *fold, double *image);
+
 /* Least-squares operator pair of the full-physics mode, in double:
    direction 0: model = L^T data (migration, [nx][ny][nh][ns], no fold);
    direction 1: data = L model (demigration, [ntr][ns]), its exact transpose. */

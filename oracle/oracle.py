@@ -51,6 +51,9 @@ def lib() -> C.CDLL:
         _lib.ko_aliasfilter.restype = C.c_int
         _lib.ko_aliasfilter.argtypes = [C.c_int, C.c_float, C.c_double, C.c_double, C.c_double,
                                         C.POINTER(C.c_int), C.c_void_p]
+        _lib.ko_kirchhoff64.restype = C.c_int
+        _lib.ko_kirchhoff64.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.ko_lsm_apply.restype = C.c_int
         _lib.ko_lsm_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p,
                                       C.c_void_p]
@@ -122,4 +125,23 @@ def lsm_apply(survey, direction: int, vec: np.ndarray, params: dict | None = Non
                             src.ctypes.data, out.ctypes.data)
     if st:
         raise RuntimeError(f"ko_lsm_apply: status {st}")
+    return out
+
+
+def kirchhoff64(survey, params: dict | None = None):
+    """FP64 oracle job: dict(image, km, fold) as float64 [nx, ny, nh, ns]."""
+    from random_gb300 import capi, segy
+    p = dict(survey.params)
+    if params:
+        p.update(params)
+    prm = capi.make_params(p)
+    vel, _keep = capi.make_velocity(survey.velocity)
+    dims = capi.oracle_dims(p)
+    out = {k: np.zeros(dims["shape"], np.float64) for k in ("image", "km", "fold")}
+    hdr = np.ascontiguousarray(segy.headers_be(survey.headers))
+    smp = np.ascontiguousarray(survey.samples, np.float32)
+    st = lib().ko_kirchhoff64(C.addressof(prm), C.addressof(vel), hdr.ctypes.data, smp.ctypes.data, survey.ntr,
+                              out["km"].ctypes.data, out["fold"].ctypes.data, out["image"].ctypes.data)
+    if st:
+        raise RuntimeError(f"ko_kirchhoff64: status {st}")
     return out

@@ -60,6 +60,11 @@ class KpstmProfile(C.Structure):
                 ("finish_ms", C.c_double), ("other_launches", C.c_int64)]
 
 
+class KpstmLaunch(C.Structure):
+    _fields_ = [("tile_px", C.c_int32), ("samples_per_lane", C.c_int32), ("persistent", C.c_int32),
+                ("graph", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
 class KpstmDims(C.Structure):
     _fields_ = [
         ("Nx", C.c_int32), ("Ny", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
@@ -141,6 +146,10 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_set_stream", C.c_int, [_VOIDP, _VOIDP])
     _sig(lib, "kpstm_profile_enable", C.c_int, [_VOIDP, C.c_int])
     _sig(lib, "kpstm_profile_read", C.c_int, [_VOIDP, C.POINTER(KpstmProfile)])
+    _sig(lib, "kpstm_get_launch", C.c_int, [_VOIDP, C.POINTER(KpstmLaunch)])
+    _sig(lib, "kpstm_set_launch", C.c_int, [_VOIDP, C.POINTER(KpstmLaunch)])
+    _sig(lib, "kpstm_autotune", C.c_int, [_VOIDP, _VOIDP, _VOIDP, i64, C.POINTER(KpstmLaunch),
+                                         C.POINTER(C.c_float)])
     _sig(lib, "kpstm_lsm_geometry", C.c_int, [_VOIDP, _VOIDP, i64])
     _sig(lib, "kpstm_lsm_adjoint", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_lsm_forward", C.c_int, [_VOIDP, _VOIDP, _VOIDP])

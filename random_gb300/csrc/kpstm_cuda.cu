@@ -26,6 +26,14 @@
         }                                                                                                    \
     } while (0)
 
+#define KP_GRAPHS 4 /* cached block graphs (two staging slots x full / last block) */
+struct kp_graph {
+    cudaGraphExec_t exec;
+    int64_t ntr;
+    const void *hdr, *smp;
+    uint64_t used;
+};
+
 struct kpstm_ctx {
     kpstm_params p;
     kpstm_setup s;
@@ -34,8 +42,19 @@ struct kpstm_ctx {
     cudaStream_t cs, xs;         /* compute, copy */
     cudaEvent_t copy_done[2], comp_done[2];
     int slot;
-    int K, nwin, ntile;
+    int K, nwin;                 /* samples per lane, time windows */
+    int64_t ntile;               /* image tiles of 8 columns */
+    int tile_px;                 /* tile patch: tile_px x (8 / tile_px) columns */
+    int persistent, use_graph;   /* launch configuration (kpstm_launch) */
+    int dirty;                   /* traces imaged since create / reset */
+    int nsm;                     /* multiprocessors of the device */
     int64_t row;                 /* floats per tap-table row */
+    int32_t *d_tilecols;         /* [ntile][8] column of each warp, -1: none */
+    int *d_queue;                /* persistent launch: work-item counter */
+    int32_t *d_clsorder;         /* persistent launch: classes by size */
+    float *h_colxy;              /* [ncol][2] column coordinates (tile boxes) */
+    kp_graph graphs[KP_GRAPHS];
+    uint64_t graph_clock;
     /* constant tables */
     float2 *d_colxy;
     int32_t *d_colrow;
@@ -55,6 +74,8 @@ struct kpstm_ctx {
     kpstm_geom *d_graw, *d_geom;
     int32_t *d_cls, *d_order, *d_cstart, *d_nlive;
     float *d_table;
+    uint16_t *d_smp16;           /* precision mode: the block's traces as bf16 */
+    float *d_scl16;              /* and their per-trace scales */
     /* staging (two slots) */
     int64_t scap;
     int32_t *d_hdr[2];
@@ -70,9 +91,13 @@ struct kpstm_ctx {
     int64_t lsm_ntr, lsm_nlive, lrow;
     kpstm_geom *d_lgraw, *d_lgeom;
     int32_t *d_lcls, *d_lorder, *d_lcstart, *d_lnlive, *d_lcnt;
-    float *d_ltable, *d_lkm;
+    float *d_ltable, *d_lkm, *d_lkc;
     unsigned long long *d_lhits;
     double *d_dotpart, *d_dot;
+    unsigned int *d_absmax;      /* demigration: bits of max |model| */
+    float *d_dbound;             /* demigration: per live trace max_k (L 1)[k] */
+    unsigned long long *d_dacc;  /* demigration: [nlive][ng] fixed-point trace accumulators */
+    int dbound_ok;
     /* stream handling / profiling */
     cudaStream_t own_cs;
     int prof;
@@ -120,41 +145,199 @@ static void prof_end(kpstm_ctx *c, int i, int stage, int launches)
 
 static int kp_free_all(kpstm_ctx *c);
 
-static size_t image_smem(const kpstm_ctx *c)
+/* ---- imaging launch ------------------------------------------------------- */
+
+static size_t image_smem_row(const kpstm_ctx *c, int64_t row, uint32_t *bar_offset)
 {
-    const int W = 32 * c->K;
     const int TB = c->p.mode == KPSTM_MODE_FULL ? KP_TB_FULL : KP_TB_REF;
-    size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * 2 * TB * c->row +
-               sizeof(int32_t) * (KP_LCH + 8 + 2);
-    b = (b + 7) & ~size_t(7);
-    return b + 2 * sizeof(uint64_t);
+    return kp_image_smem(c->K, TB, row, bar_offset);
 }
 
+typedef void (*kp_image_fn)(KpImageArgs);
+
 template <int K>
-static cudaError_t launch_image_k(const kpstm_ctx *c, const KpImageArgs &a, dim3 grid, size_t smem)
+static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo)
+{
+    if (hilo) {
+        if constexpr (K <= 16) {
+            if (kahan) return k_image<K, true, true, true>;
+        }
+        if constexpr (K <= 24) {
+            if (!kahan) return k_image<K, true, false, true>;
+        }
+        return nullptr;
+    }
+    if (kahan) {
+        if constexpr (K <= 16) return full ? k_image<K, true, true> : k_image<K, false, true>;
+        return nullptr;
+    }
+    if (full) {
+        if constexpr (K <= 24) return k_image<K, true, false>;
+        return nullptr;
+    }
+    return k_image<K, false, false>;
+}
+
+static kp_image_fn image_fn(const kpstm_ctx *c, bool hilo)
 {
     const bool full = c->p.mode == KPSTM_MODE_FULL;
     const bool kahan = c->p.precision == KPSTM_PREC_BF16_KAHAN;
-    void (*fn)(KpImageArgs);
-    if (full)
-        fn = kahan ? k_image<K, true, true> : k_image<K, true, false>;
-    else
-        fn = kahan ? k_image<K, false, true> : k_image<K, false, false>;
+    switch (c->K) {
+    case 8: return image_fn_k<8>(full, kahan, hilo);
+    case 16: return image_fn_k<16>(full, kahan, hilo);
+    case 24: return image_fn_k<24>(full, kahan, hilo);
+    default: return image_fn_k<32>(full, kahan, hilo);
+    }
+}
+
+/* Launches the imaging kernel over nclass classes of the args' table.
+   Grid mode: one CTA per (tile, class, window).  Persistent mode: the
+   classes are ranked by size on the device, the work counter is cleared and
+   a grid of the resident CTAs drains the items. */
+static cudaError_t launch_image(kpstm_ctx *c, KpImageArgs a, int nclass, bool hilo)
+{
+    kp_image_fn fn = image_fn(c, hilo);
+    if (!fn) return cudaErrorInvalidValue;
+    size_t smem = image_smem_row(c, a.row, &a.bar_offset);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    fn<<<grid, KP_THREADS, smem, c->cs>>>(a);
+    a.ntile = c->ntile;
+    a.nwin = c->nwin;
+    a.tilecols = c->d_tilecols;
+    a.tilebox = c->d_tilebox;
+    const int64_t nitems = (int64_t)nclass * c->ntile * c->nwin;
+    if (nitems == 0) return cudaSuccess;
+    if (c->persistent && nitems < INT32_MAX) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, KP_THREADS, smem);
+        if (e != cudaSuccess) return e;
+        if (occ < 1) occ = 1;
+        int64_t grid = (int64_t)occ * c->nsm;
+        if (grid > nitems) grid = nitems;
+        k_class_order<<<1, 1024, 0, c->cs>>>(a.class_start, nclass, c->d_clsorder);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_queue, 0, sizeof(int), c->cs);
+        if (e != cudaSuccess) return e;
+        a.queue = c->d_queue;
+        a.nitems = (int)nitems;
+        a.cls_order = c->d_clsorder;
+        fn<<<(unsigned)grid, KP_THREADS, smem, c->cs>>>(a);
+    } else {
+        if (c->ntile > INT32_MAX || nclass > 65535 || c->nwin > 65535) return cudaErrorInvalidValue;
+        fn<<<dim3(c->ntile, nclass, c->nwin), KP_THREADS, smem, c->cs>>>(a);
+    }
     return cudaGetLastError();
 }
 
-static cudaError_t launch_image(const kpstm_ctx *c, const KpImageArgs &a)
+/* Largest samples-per-lane the mode's register budget allows (2 CTAs/SM,
+   128 registers, no spills): reference 32, full 24, Kahan variants 16. */
+static int kmax_of(const kpstm_params *p)
 {
-    dim3 grid(c->ntile, c->s.nclass, c->nwin);
-    size_t smem = image_smem(c);
-    switch (c->K) {
-    case 8: return launch_image_k<8>(c, a, grid, smem);
-    case 16: return launch_image_k<16>(c, a, grid, smem);
-    case 24: return launch_image_k<24>(c, a, grid, smem);
-    default: return launch_image_k<32>(c, a, grid, smem);
+    if (p->precision == KPSTM_PREC_BF16_KAHAN) return 16;
+    return p->mode == KPSTM_MODE_FULL ? 24 : 32;
+}
+
+static int default_K(const kpstm_params *p)
+{
+    const int kmax = kmax_of(p);
+    const int nwin = (p->ns + 32 * kmax - 1) / (32 * kmax);
+    const int per = (p->ns + nwin - 1) / nwin;
+    return per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
+}
+
+/* default patch: the fewest tiles (fewest idle warps), ties to the
+   consecutive-crossline patch 1 x 8 */
+static int default_px(const kpstm_setup *s)
+{
+    int best = 1;
+    int64_t bn = -1;
+    for (int px = 1; px <= 8; px *= 2) {
+        const int py = 8 / px;
+        const int64_t n = (int64_t)((s->dims.nx + px - 1) / px) * ((s->dims.ny + py - 1) / py);
+        if (bn < 0 || n < bn) {
+            bn = n;
+            best = px;
+        }
+    }
+    return best;
+}
+
+/* (Re)builds the tile -> column map and the tiles' bounding boxes for
+   tile_px x (8 / tile_px) patches. */
+static int set_tiles(kpstm_ctx *c, int px)
+{
+    const int nx = c->s.dims.nx, ny = c->s.dims.ny, py = 8 / px;
+    const int ntx = (nx + px - 1) / px, nty = (ny + py - 1) / py;
+    const int64_t ntile = (int64_t)ntx * nty;
+    int32_t *cols = (int32_t *)malloc(sizeof(int32_t) * KPSTM_COLS_PER_CTA * ntile);
+    float4 *box = (float4 *)malloc(sizeof(float4) * ntile);
+    if (!cols || !box) {
+        free(cols);
+        free(box);
+        return KPSTM_ERR_OUT_OF_MEMORY;
+    }
+    for (int tx = 0; tx < ntx; ++tx)
+        for (int ty = 0; ty < nty; ++ty) {
+            const int64_t t = (int64_t)tx * nty + ty;
+            float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+            for (int w = 0; w < KPSTM_COLS_PER_CTA; ++w) {
+                const int xc = tx * px + w / py, yc = ty * py + w % py;
+                int32_t col = -1;
+                if (xc < nx && yc < ny) {
+                    col = xc * ny + yc;
+                    const float X = c->h_colxy[2 * col], Y = c->h_colxy[2 * col + 1];
+                    x0 = fminf(x0, X);
+                    x1 = fmaxf(x1, X);
+                    y0 = fminf(y0, Y);
+                    y1 = fmaxf(y1, Y);
+                }
+                cols[t * KPSTM_COLS_PER_CTA + w] = col;
+            }
+            box[t] = make_float4(x0, x1, y0, y1);
+        }
+    int st = KPSTM_OK;
+    do {
+        if (cudaStreamSynchronize(c->cs) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        if (ntile != c->ntile || !c->d_tilecols) {
+            cudaFree(c->d_tilecols);
+            cudaFree(c->d_tilebox);
+            c->d_tilecols = nullptr;
+            c->d_tilebox = nullptr;
+            c->ntile = 0;
+            if (cudaMalloc(&c->d_tilecols, sizeof(int32_t) * KPSTM_COLS_PER_CTA * ntile) != cudaSuccess ||
+                cudaMalloc(&c->d_tilebox, sizeof(float4) * ntile) != cudaSuccess) {
+                st = KPSTM_ERR_OUT_OF_MEMORY;
+                break;
+            }
+        }
+        if (cudaMemcpy(c->d_tilecols, cols, sizeof(int32_t) * KPSTM_COLS_PER_CTA * ntile, cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaMemcpy(c->d_tilebox, box, sizeof(float4) * ntile, cudaMemcpyHostToDevice) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        c->ntile = ntile;
+        c->tile_px = px;
+    } while (0);
+    free(cols);
+    free(box);
+    return st;
+}
+
+static void set_K(kpstm_ctx *c, int K)
+{
+    c->K = K;
+    c->nwin = (c->p.ns + 32 * K - 1) / (32 * K);
+}
+
+static void drop_graphs(kpstm_ctx *c)
+{
+    for (int i = 0; i < KP_GRAPHS; ++i) {
+        if (c->graphs[i].exec) cudaGraphExecDestroy(c->graphs[i].exec);
+        c->graphs[i].exec = nullptr;
     }
 }
 
@@ -162,14 +345,19 @@ static int grow_work(kpstm_ctx *c, int64_t ntr)
 {
     if (ntr <= c->cap) return KPSTM_OK;
     KP_CUDA(cudaStreamSynchronize(c->cs));
+    drop_graphs(c); /* they hold the old buffers */
     cudaFree(c->d_graw);
     cudaFree(c->d_geom);
     cudaFree(c->d_cls);
     cudaFree(c->d_order);
     cudaFree(c->d_table);
+    cudaFree(c->d_smp16);
+    cudaFree(c->d_scl16);
     c->d_graw = c->d_geom = nullptr;
     c->d_cls = c->d_order = nullptr;
     c->d_table = nullptr;
+    c->d_smp16 = nullptr;
+    c->d_scl16 = nullptr;
     c->cap = 0;
     int64_t n = ntr + ntr / 8 + 64;
     KP_CUDA(cudaMalloc(&c->d_graw, sizeof(kpstm_geom) * n));
@@ -177,6 +365,10 @@ static int grow_work(kpstm_ctx *c, int64_t ntr)
     KP_CUDA(cudaMalloc(&c->d_cls, sizeof(int32_t) * n));
     KP_CUDA(cudaMalloc(&c->d_order, sizeof(int32_t) * n));
     KP_CUDA(cudaMalloc(&c->d_table, sizeof(float) * c->row * n));
+    if (c->p.precision == KPSTM_PREC_BF16_KAHAN) {
+        KP_CUDA(cudaMalloc(&c->d_smp16, sizeof(uint16_t) * c->p.ns * n));
+        KP_CUDA(cudaMalloc(&c->d_scl16, sizeof(float) * n));
+    }
     c->cap = n;
     return KPSTM_OK;
 }
@@ -202,12 +394,12 @@ static int grow_stage(kpstm_ctx *c, int64_t ntr)
     return KPSTM_OK;
 }
 
-/* The per-block device pipeline on the compute stream. */
-static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int64_t ntr)
+static KpImageArgs image_args(const kpstm_ctx *c);
+
+/* The per-block device pipeline, enqueued on the compute stream (the work
+   buffers must already hold ntr traces). */
+static int enqueue_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int64_t ntr)
 {
-    if (ntr == 0) return KPSTM_OK;
-    int st = grow_work(c, ntr);
-    if (st) return st;
     const kpstm_params *p = &c->p;
     const kpstm_setup *s = &c->s;
 
@@ -240,6 +432,16 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     KpPrepArgs pa;
     memset(&pa, 0, sizeof(pa));
     pa.samples = d_smp;
+    if (p->precision == KPSTM_PREC_BF16_KAHAN) {
+        /* precision mode: the block is kept as bf16 with a per-trace scale and
+           the taps are built from it with double integrals */
+        k_to_bf16<<<(unsigned)((ntr * 32 + 255) / 256), 256, 0, c->cs>>>(d_smp, ntr, p->ns, c->d_smp16, c->d_scl16);
+        KP_CUDA(cudaGetLastError());
+        pa.samples = nullptr;
+        pa.samples_bf16 = c->d_smp16;
+        pa.scale = c->d_scl16;
+        pa.exact = 1;
+    }
     pa.geom_raw = c->d_graw;
     pa.order = c->d_order;
     pa.nlive = c->d_nlive;
@@ -256,40 +458,61 @@ static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int
     KP_CUDA(cudaGetLastError());
     prof_end(c, pe, 1, 3);
 
-    KpImageArgs a;
-    memset(&a, 0, sizeof(a));
+    KpImageArgs a = image_args(c);
     a.geom = c->d_geom;
     a.class_start = c->d_cstart;
     a.table = c->d_table;
     a.row = c->row;
-    a.colxy = c->d_colxy;
-    a.colrow = c->d_colrow;
-    a.tilebox = c->d_tilebox;
-    a.vrows = c->d_vrows;
-    a.t2 = c->d_t2;
-    a.t2c = c->d_t2c;
-    a.inv_l2 = c->d_invl2;
     a.km = c->d_km;
     a.kc = c->d_kc;
     a.cnt = c->d_cnt;
     a.hits = c->d_hits;
-    a.status = c->d_status;
-    a.ncol = s->ncol;
-    a.ns = p->ns;
-    a.tm = s->dims.trange_max;
-    a.lmax = s->lmax;
-    a.lmaxf = (float)s->lmax;
-    a.dt = p->dt;
-    a.rdt = 1.0f / p->dt;
-    a.nsf = (float)p->ns;
-    a.aperture = p->aperture;
-    float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
-    a.tile_r2 = r * r;
-    a.aax = (float)p->iline_distance; /* slopes in samples per trace spacing (sample units) */
-    a.aay = (float)p->xline_distance;
     int pi = prof_begin(c);
-    KP_CUDA(launch_image(c, a));
+    KP_CUDA(launch_image(c, a, s->nclass, false));
     prof_end(c, pi, 0, 1);
+    return KPSTM_OK;
+}
+
+/* One block: directly, or (graph flag, profiling off) by replaying the
+   block's pipeline from a CUDA graph captured on first use of this
+   (ntr, buffers) shape; a few shapes are cached, least recently used out. */
+static int run_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp, int64_t ntr)
+{
+    if (ntr == 0) return KPSTM_OK;
+    int st = grow_work(c, ntr);
+    if (st) return st;
+    c->dirty = 1;
+    if (!c->use_graph || c->prof) return enqueue_block(c, d_hdr, d_smp, ntr);
+    kp_graph *g = nullptr, *victim = &c->graphs[0];
+    for (int i = 0; i < KP_GRAPHS; ++i) {
+        kp_graph *q = &c->graphs[i];
+        if (q->exec && q->ntr == ntr && q->hdr == d_hdr && q->smp == d_smp) g = q;
+        if (!q->exec || (victim->exec && q->used < victim->used)) victim = q;
+    }
+    if (!g) {
+        if (victim->exec) cudaGraphExecDestroy(victim->exec);
+        victim->exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        KP_CUDA(cudaStreamBeginCapture(c->cs, cudaStreamCaptureModeThreadLocal));
+        st = enqueue_block(c, d_hdr, d_smp, ntr);
+        cudaError_t e = cudaStreamEndCapture(c->cs, &graph);
+        if (st || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return st ? st : KPSTM_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&victim->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            victim->exec = nullptr;
+            return KPSTM_ERR_CUDA;
+        }
+        victim->ntr = ntr;
+        victim->hdr = d_hdr;
+        victim->smp = d_smp;
+        g = victim;
+    }
+    g->used = ++c->graph_clock;
+    KP_CUDA(cudaGraphLaunch(g->exec, c->cs));
     return KPSTM_OK;
 }
 
@@ -314,16 +537,15 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     cudaGetDevice(&c->device);
     const int ns = params->ns, tm = s.dims.trange_max;
     const int ncol = s.ncol;
-    /* samples per lane: as many as fit the 128-register budget of 2 CTAs/SM
-       without spilling (reference 32, full 24, Kahan variants 8 fewer) */
-    const bool fullm = params->mode == KPSTM_MODE_FULL, kah = params->precision == KPSTM_PREC_BF16_KAHAN;
-    const int kmax = (fullm ? 24 : 32) - (kah ? 8 : 0);
-    c->nwin = (ns + 32 * kmax - 1) / (32 * kmax);
-    int per = (ns + c->nwin - 1) / c->nwin;
-    c->K = per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
-    c->ntile = (ncol + KPSTM_COLS_PER_CTA - 1) / KPSTM_COLS_PER_CTA;
+    set_K(c, default_K(params));
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c->nsm < 1)
+            c->nsm = 1;
+    }
     if (params->mode == KPSTM_MODE_FULL)
-        c->row = ((2 * (int64_t)(ns + 2 * tm - 3)) + 3) & ~int64_t(3);
+        c->row = ((2 * (int64_t)(ns + 2 * tm - 2)) + 3) & ~int64_t(3); /* entries 0 .. ns + 2tm - 3 */
     else
         c->row = (ns + 1 + 3) & ~3; /* D[0..ns-1] plus a zero sentinel D[ns] */
 
@@ -338,13 +560,12 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     float *tsc = (float *)malloc(sizeof(float) * ns);
     double *hd = (double *)malloc(sizeof(double) * ns);
     float *hf = (float *)malloc(sizeof(float) * ns);
-    float4 *box = (float4 *)malloc(sizeof(float4) * c->ntile);
     int32_t *rowmap = nullptr;
     float2 *vrows = nullptr;
     float invl2[64];
     int nrow = 0;
     do {
-        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !tsc || !hd || !hf || !box) {
+        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !tsc || !hd || !hf) {
             st = KPSTM_ERR_OUT_OF_MEMORY;
             break;
         }
@@ -364,18 +585,6 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
         st = kpstm_lowpass_kernel(params, hd);
         if (st) break;
         for (int t = 0; t < ns; ++t) hf[t] = (float)hd[t];
-        for (int b = 0; b < c->ntile; ++b) {
-            float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
-            for (int k = 0; k < KPSTM_COLS_PER_CTA; ++k) {
-                int cc = b * KPSTM_COLS_PER_CTA + k;
-                if (cc >= ncol) break;
-                x0 = fminf(x0, colxy[2 * cc]);
-                x1 = fmaxf(x1, colxy[2 * cc]);
-                y0 = fminf(y0, colxy[2 * cc + 1]);
-                y1 = fmaxf(y1, colxy[2 * cc + 1]);
-            }
-            box[b] = make_float4(x0, x1, y0, y1);
-        }
         /* compact the velocity rows the slab uses; v^2 in float as
            Kirchhoff.c:617, RN(1/v^2) for the exact division */
         int64_t ngrid = (int64_t)vel->n_iline * vel->n_xline;
@@ -429,7 +638,8 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     }
             KP_ALLOC(c->d_colxy, sizeof(float2) * ncol);
             KP_ALLOC(c->d_colrow, sizeof(int32_t) * ncol);
-            KP_ALLOC(c->d_tilebox, sizeof(float4) * c->ntile);
+            KP_ALLOC(c->d_queue, sizeof(int));
+            KP_ALLOC(c->d_clsorder, sizeof(int32_t) * s.nclass);
             KP_ALLOC(c->d_vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns);
             KP_ALLOC(c->d_t2, sizeof(float) * ns);
             KP_ALLOC(c->d_t2c, sizeof(float2) * ns);
@@ -448,7 +658,6 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
 #undef KP_ALLOC
             cudaMemcpyAsync(c->d_colxy, colxy, sizeof(float2) * ncol, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_colrow, colrow, sizeof(int32_t) * ncol, cudaMemcpyHostToDevice, c->cs);
-            cudaMemcpyAsync(c->d_tilebox, box, sizeof(float4) * c->ntile, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_vrows, vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns,
                             cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_t2, t2, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
@@ -463,7 +672,13 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             if (c->d_kc) cudaMemsetAsync(c->d_kc, 0, sizeof(float) * nimg, c->cs);
             cudaMemsetAsync(c->d_status, 0, sizeof(int), c->cs);
             cudaMemsetAsync(c->d_hits, 0, sizeof(unsigned long long), c->cs);
-            if (cudaStreamSynchronize(c->cs) != cudaSuccess) st = KPSTM_ERR_CUDA;
+            if (cudaStreamSynchronize(c->cs) != cudaSuccess) {
+                st = KPSTM_ERR_CUDA;
+                break;
+            }
+            c->h_colxy = colxy;
+            colxy = nullptr;
+            st = set_tiles(c, default_px(&s));
         } while (0);
     }
     free(colxy);
@@ -476,7 +691,6 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     free(tsc);
     free(hd);
     free(hf);
-    free(box);
     free(rowmap);
     free(vrows);
     if (st) {
@@ -498,13 +712,16 @@ static int kp_free_all(kpstm_ctx *c)
                     c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
                     c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
                     c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
-                    c->d_lhits, c->d_dotpart, c->d_dot};
+                    c->d_lhits, c->d_dotpart, c->d_dot, c->d_smp16, c->d_scl16, c->d_tilecols, c->d_queue,
+                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
         if (c->copy_done[k]) cudaEventDestroy(c->copy_done[k]);
         if (c->comp_done[k]) cudaEventDestroy(c->comp_done[k]);
     }
+    drop_graphs(c);
+    free(c->h_colxy);
     for (int i = 0; i < c->nev; ++i) cudaEventDestroy(c->ev[i]);
     free(c->ev);
     free(c->evstage);
@@ -550,6 +767,7 @@ extern "C" int kpstm_reset(kpstm_ctx *c)
     KP_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->cs));
     KP_CUDA(cudaMemsetAsync(c->d_hits, 0, sizeof(unsigned long long), c->cs));
     KP_CUDA(cudaStreamSynchronize(c->cs));
+    c->dirty = 0;
     return KPSTM_OK;
 }
 
@@ -785,6 +1003,110 @@ extern "C" int kpstm_profile_read(kpstm_ctx *c, kpstm_profile *out)
 }
 
 /* ------------------------------------------------------------------------ */
+/* Launch configuration and autotuner (kpstm_launch). */
+
+extern "C" int kpstm_get_launch(const kpstm_ctx *c, kpstm_launch *cfg)
+{
+    if (!c || !cfg) return KPSTM_ERR_INVALID_ARG;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->tile_px = c->tile_px;
+    cfg->samples_per_lane = c->K;
+    cfg->persistent = c->persistent;
+    cfg->graph = c->use_graph;
+    return KPSTM_OK;
+}
+
+static bool valid_K(const kpstm_ctx *c, int K)
+{
+    return (K == 8 || K == 16 || K == 24 || K == 32) && K <= kmax_of(&c->p);
+}
+
+extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
+{
+    if (!c || !cfg) return KPSTM_ERR_INVALID_ARG;
+    const int px = cfg->tile_px ? cfg->tile_px : default_px(&c->s);
+    const int K = cfg->samples_per_lane ? cfg->samples_per_lane : default_K(&c->p);
+    if ((px != 1 && px != 2 && px != 4 && px != 8) || !valid_K(c, K)) return KPSTM_ERR_INVALID_ARG;
+    if ((cfg->persistent != 0 && cfg->persistent != 1) || (cfg->graph != 0 && cfg->graph != 1))
+        return KPSTM_ERR_INVALID_ARG;
+    drop_graphs(c);
+    if (px != c->tile_px) {
+        int st = set_tiles(c, px);
+        if (st) return st;
+    }
+    set_K(c, K);
+    c->persistent = cfg->persistent;
+    c->use_graph = cfg->graph;
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_autotune(kpstm_ctx *c, const int32_t *d_hdr_be, const float *d_samples, int64_t ntr,
+                              kpstm_launch *best, float *best_ms)
+{
+    if (!c || ntr <= 0 || !d_hdr_be || !d_samples || ntr > INT32_MAX / 2) return KPSTM_ERR_INVALID_ARG;
+    if (c->dirty) return KPSTM_ERR_STATE;
+    int st = grow_work(c, ntr);
+    if (st) return st;
+    const int prof = c->prof, graph = c->use_graph;
+    c->prof = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) st = KPSTM_ERR_CUDA;
+    /* patches with at most twice the fewest tiles (others leave most warps idle) */
+    int64_t nmin = -1;
+    for (int px = 1; px <= 8; px *= 2) {
+        const int py = 8 / px;
+        const int64_t n = (int64_t)((c->s.dims.nx + px - 1) / px) * ((c->s.dims.ny + py - 1) / py);
+        if (nmin < 0 || n < nmin) nmin = n;
+    }
+    kpstm_launch win;
+    memset(&win, 0, sizeof(win));
+    float win_ms = -1.0f;
+    for (int px = 1; px <= 8 && !st; px *= 2) {
+        const int py = 8 / px;
+        const int64_t n = (int64_t)((c->s.dims.nx + px - 1) / px) * ((c->s.dims.ny + py - 1) / py);
+        if (n > 2 * nmin) continue;
+        for (int K = 8; K <= 32 && !st; K += 8) {
+            if (!valid_K(c, K)) continue;
+            for (int pers = 0; pers <= 1 && !st; ++pers) {
+                kpstm_launch cfg;
+                memset(&cfg, 0, sizeof(cfg));
+                cfg.tile_px = px;
+                cfg.samples_per_lane = K;
+                cfg.persistent = pers;
+                st = kpstm_set_launch(c, &cfg);
+                if (st) break;
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2 && !st; ++rep) { /* the first run warms caches and attributes */
+                    if (cudaEventRecord(e0, c->cs) != cudaSuccess) st = KPSTM_ERR_CUDA;
+                    if (!st) st = enqueue_block(c, d_hdr_be, d_samples, ntr);
+                    if (!st && (cudaEventRecord(e1, c->cs) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                        st = KPSTM_ERR_CUDA;
+                }
+                if (!st) st = check_status(c);
+                if (!st && (win_ms < 0.0f || ms < win_ms)) {
+                    win_ms = ms;
+                    win = cfg;
+                }
+            }
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    c->prof = prof;
+    if (!st) {
+        win.graph = graph;
+        st = kpstm_set_launch(c, &win);
+    }
+    int st2 = kpstm_reset(c);
+    if (!st) st = st2;
+    if (st) return st;
+    if (best) *best = win;
+    if (best_ms) *best_ms = win_ms;
+    return KPSTM_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Finishing without device allocation (kpstm_finish_noalloc).
    The scratch a finishing pass needs - the derivative traces between
    k_deriv and k_lowpass, and the low-pass impulse response - is this one
@@ -925,16 +1247,6 @@ static KpImageArgs image_args(const kpstm_ctx *c)
     return a;
 }
 
-template <int K>
-static cudaError_t launch_image_hilo_k(const kpstm_ctx *c, const KpImageArgs &a, dim3 grid, size_t smem)
-{
-    void (*fn)(KpImageArgs) = k_image<K, true, false, true>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    fn<<<grid, KP_THREADS, smem, c->cs>>>(a);
-    return cudaGetLastError();
-}
-
 static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d_data16, const float *d_scale,
                             float *d_model)
 {
@@ -942,6 +1254,7 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
     const size_t nimg = (size_t)ncls * ncol * ns;
     KP_CUDA(cudaMemsetAsync(c->d_lkm, 0, sizeof(float) * nimg, c->cs));
     KP_CUDA(cudaMemsetAsync(c->d_lcnt, 0, sizeof(int32_t) * nimg, c->cs));
+    if (c->d_lkc) KP_CUDA(cudaMemsetAsync(c->d_lkc, 0, sizeof(float) * nimg, c->cs));
     if (c->lsm_nlive > 0) {
         KpPrepArgs pa;
         memset(&pa, 0, sizeof(pa));
@@ -969,19 +1282,10 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
         a.table = c->d_ltable;
         a.row = c->lrow;
         a.km = c->d_lkm;
+        a.kc = c->d_lkc;
         a.cnt = c->d_lcnt;
         a.hits = c->d_lhits;
-        const int W = 32 * c->K;
-        size_t smem = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W +
-                      sizeof(float) * 2 * KP_TB_FULL * c->lrow + sizeof(int32_t) * (KP_LCH + 8 + 2);
-        smem = ((smem + 7) & ~size_t(7)) + 2 * sizeof(uint64_t);
-        dim3 grid(c->ntile, ncls, c->nwin);
-        cudaError_t e;
-        switch (c->K) {
-        case 8: e = launch_image_hilo_k<8>(c, a, grid, smem); break;
-        case 16: e = launch_image_hilo_k<16>(c, a, grid, smem); break;
-        default: e = launch_image_hilo_k<24>(c, a, grid, smem); break;
-        }
+        cudaError_t e = launch_image(c, a, ncls, true);
         KP_CUDA(e);
     }
     k_relayout<<<1024, 256, 0, c->cs>>>(c->d_lkm, nullptr, c->d_tscale, ncol, ncls, ns, d_model);
@@ -1025,10 +1329,39 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.rdt2 = rdt * rdt;
     a.aax = (float)p->iline_distance;
     a.aay = (float)p->xline_distance;
-    const size_t smem = sizeof(float) * 8 * (size_t)((ns + 3) & ~3);
+    a.dt = p->dt;
+    a.ng = ns + s->dims.trange_max - 1; /* G index <= ns - 1 + lmax, lmax <= tm - 1 */
+    /* |d| 2^E < 2^63 needs (columns x samples x lmax) < 2^33 (worst case: every
+       pair of the trace covering one sample with weight bound and width lmax) */
+    const double cover = (double)s->ncol * ns * (s->lmax > 1 ? s->lmax : 1);
+    a.shift = cover > 8589934592.0 ? (int)ceil(log2(cover / 8589934592.0)) : 0;
+    a.absmax = c->d_absmax;
+    const size_t smem = sizeof(unsigned long long) * KP_DM_WARPS * (size_t)a.ng + sizeof(float) * 2 * (size_t)ns;
     if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
+    const size_t accb = sizeof(unsigned long long) * (size_t)a.ng * (size_t)c->lsm_nlive;
+    if (!c->d_dacc) {
+        if (cudaMalloc(&c->d_dacc, accb) != cudaSuccess) return KPSTM_ERR_OUT_OF_MEMORY;
+    }
+    a.acc = c->d_dacc;
     KP_CUDA(cudaFuncSetAttribute(k_demig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_demig<<<(unsigned)((c->lsm_nlive + 7) / 8), 256, smem, c->cs>>>(a);
+    const unsigned nblk = (unsigned)((c->lsm_nlive + KP_DM_WARPS - 1) / KP_DM_WARPS);
+    if (!c->dbound_ok) {
+        /* once per geometry: max_k (L 1)[trace, k], the fixed-point range of each trace */
+        KpDemigArgs b = a;
+        b.model = nullptr;
+        b.dbound_out = c->d_dbound;
+        KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
+        k_demig<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
+        KP_CUDA(cudaGetLastError());
+        c->dbound_ok = 1;
+    }
+    KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
+    a.dbound = c->d_dbound;
+    const int64_t nmodel = (int64_t)s->nclass * s->ncol * ns;
+    KP_CUDA(cudaMemsetAsync(c->d_absmax, 0, sizeof(unsigned int), c->cs));
+    k_absmax<<<4 * c->nsm, 256, 0, c->cs>>>(d_model, nmodel, c->d_absmax);
+    KP_CUDA(cudaGetLastError());
+    k_demig<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(a);
     KP_CUDA(cudaGetLastError());
     return KPSTM_OK;
 }
@@ -1039,9 +1372,15 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
     if (c->p.mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED;
     KP_CUDA(cudaStreamSynchronize(c->cs));
     void *old[] = {c->d_lgraw, c->d_lgeom, c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive,
-                   c->d_lcnt, c->d_ltable, c->d_lkm, c->d_lhits, c->d_dotpart, c->d_dot};
+                   c->d_lcnt, c->d_ltable, c->d_lkm, c->d_lhits, c->d_dotpart, c->d_dot, c->d_absmax,
+                   c->d_dbound, c->d_lkc, c->d_dacc};
     for (size_t i = 0; i < sizeof(old) / sizeof(old[0]); ++i)
         if (old[i]) cudaFree(old[i]);
+    c->d_lkc = nullptr;
+    c->d_dacc = nullptr;
+    c->d_absmax = nullptr;
+    c->d_dbound = nullptr;
+    c->dbound_ok = 0;
     c->d_lgraw = c->d_lgeom = nullptr;
     c->d_lcls = c->d_lorder = c->d_lcstart = c->d_lnlive = c->d_lcnt = nullptr;
     c->d_ltable = c->d_lkm = nullptr;
@@ -1070,6 +1409,9 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         KP_LALLOC(c->d_lhits, sizeof(unsigned long long));
         KP_LALLOC(c->d_dotpart, sizeof(double) * KP_DOT_BLOCKS);
         KP_LALLOC(c->d_dot, sizeof(double) * 4);
+        KP_LALLOC(c->d_absmax, sizeof(unsigned int));
+        KP_LALLOC(c->d_dbound, sizeof(float) * (size_t)ntr);
+        if (c->p.precision == KPSTM_PREC_BF16_KAHAN) KP_LALLOC(c->d_lkc, sizeof(float) * nimg);
 #undef KP_LALLOC
         if (cudaMemcpyAsync(d_hdr, hdr_be, sizeof(int32_t) * 60 * ntr, cudaMemcpyHostToDevice, c->cs) !=
             cudaSuccess) {
@@ -1109,7 +1451,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         }
         c->lsm_ntr = ntr;
         c->lsm_nlive = nl;
-        c->lrow = ((4 * (int64_t)(ns + 2 * tm - 3)) + 3) & ~int64_t(3);
+        c->lrow = 4 * (int64_t)(ns + 2 * tm - 2);
         if (cudaMalloc(&c->d_ltable, sizeof(float) * c->lrow * (size_t)(nl > 0 ? nl : 1)) != cudaSuccess) {
             st = KPSTM_ERR_OUT_OF_MEMORY;
             break;

@@ -47,6 +47,7 @@ struct KpPrepArgs {
     const double *c4r;             /* [ns] RN(1/(4*t2[t])) */
     int64_t row;                   /* floats per table row */
     int ns, tm, full, hilo;        /* hilo: full-mode rows of float4 {hi, lo, dP, 0} */
+    int exact;                     /* reference-mode taps from double integrals (precision mode) */
     float dt;
 };
 
@@ -71,7 +72,13 @@ struct KpImageArgs {
     float dt, rdt, nsf, lmaxf;
     double aperture;
     float tile_r2;                 /* squared tile-test radius (aperture + margin) */
-    float aax, aay;                /* full mode: line spacing / dt */
+    float aax, aay;                /* full mode: line spacings */
+    const int32_t *tilecols;       /* [ntile][8] column of each warp, -1 = none */
+    int ntile, nwin;
+    uint32_t bar_offset;           /* byte offset of the two mbarriers in shared memory */
+    int *queue;                    /* persistent mode: work-item counter (zeroed per launch) */
+    int nitems;                    /* persistent mode: ntile * nwin * classes */
+    const int32_t *cls_order;      /* persistent mode: classes, largest first */
 };
 
 /* ------------------------------------------------------------------------ */
@@ -192,6 +199,25 @@ __global__ void __launch_bounds__(1024) k_bucket(const int32_t *cls, int64_t ntr
     }
 }
 
+/* Classes by decreasing trace count (ties: lower class first), for the
+   persistent imaging launch: cls_order[r] is the class of rank r.  One CTA,
+   ncls <= KPSTM_MAX_CLASSES. */
+__global__ void __launch_bounds__(1024) k_class_order(const int32_t *class_start, int ncls, int32_t *cls_order)
+{
+    __shared__ int32_t sz[KPSTM_MAX_CLASSES];
+    for (int c = threadIdx.x; c < ncls; c += blockDim.x) sz[c] = class_start[c + 1] - class_start[c];
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncls; c += blockDim.x) {
+        const int mine = sz[c];
+        int r = 0;
+        for (int j = 0; j < ncls; ++j) {
+            const int o = sz[j];
+            r += (o > mine) || (o == mine && j < c);
+        }
+        cls_order[r] = c;
+    }
+}
+
 /* Per-trace tap tables, one thread per trace.
    Reference mode: the running integrals of Kirchhoff.c:1312-1328 in the
    reference's order and precision - the first integral adds f[t]/(4*t2[t])
@@ -226,8 +252,10 @@ __global__ void k_prep(KpPrepArgs a)
         }
         double p1 = 0.0, p2 = 0.0;
         /* last P index stored: the imaging kernel reads entry floor(x) + tm with
-           x < ns - 2 + lmax and lmax <= tm - 1, i.e. entries 0 .. ns + 2tm - 4 */
-        const int iend = ns + tm - 4;
+           x = RN(x0 + Lf) <= ns - 2 + lmax (x0 < ns - 2, Lf <= lmax; the sum can
+           round up onto the bound) and lmax <= tm - 1, i.e. entries
+           0 .. ns + 2tm - 3 */
+        const int iend = ns + tm - 3;
         for (int t = 0; t <= iend + 1; ++t) {
             if (t < ns) p1 += (double)KP_SAMPLE(t);
             const double prev = p2;
@@ -239,6 +267,28 @@ __global__ void k_prep(KpPrepArgs a)
                 q[t - 1 + tm] = make_float2((float)prev, (float)p1); /* entry of P index t-1 */
             }
         }
+        return;
+    }
+    if (a.exact) {
+        /* the same integrals and taps, every step in double, rounded once
+           when the tap is stored (no float running sums) */
+        const double fl = (double)KP_SAMPLE(ns - 1), dtd = (double)a.dt;
+        double q1 = (double)KP_SAMPLE(0), q2 = q1;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = q2, n1 = 0.0, n2 = 0.0;
+        for (int t = 1; t < ns + 2; ++t) {
+            if (t < ns) q1 += kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]);
+            else q1 += fl / (dtd * dtd * (double)t * (double)t);
+            q2 += q1;
+            if (t == 1) n1 = q2;
+            if (t == 2) n2 = q2;
+            s0 = s1; s1 = s2; s2 = s3; s3 = s4; s4 = q2;
+            if (t >= 2) {
+                const int T = t - 2;
+                const double pm = T >= 2 ? s0 : (T == 1 ? n1 : n2);
+                if (T < ns) row[T] = (float)(-2.0 * s2 + pm + s4);
+            }
+        }
+        row[ns] = 0.0f;
         return;
     }
     const float flast = KP_SAMPLE(ns - 1);
@@ -311,17 +361,34 @@ __device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float 
     return dx * dx + dy * dy < r2;
 }
 
-template <int K, bool FULL, bool KAHAN, bool HILO = false>
-__global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
+/* Shared-memory layout of k_image: s_v (8 warps x W float2), s_t (W
+   float2), two TMA buffers of TB rows, the compaction list, 8 warp counts,
+   2 flags and 2 mbarriers.  Returns the total bytes; *bar_offset receives
+   the barriers' offset (8-byte aligned, flags right before them). */
+__host__ __device__ inline size_t kp_image_smem(int K, int TB, int64_t row, uint32_t *bar_offset)
+{
+    const size_t W = 32 * (size_t)K;
+    size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * 2 * TB * (size_t)row +
+               sizeof(int32_t) * (KP_LCH + 8);
+    b = ((b + 8 + 7) & ~size_t(7)); /* end of the two flags, 8-byte aligned */
+    if (bar_offset) *bar_offset = (uint32_t)b;
+    return b + 2 * sizeof(uint64_t);
+}
+
+/* One work item of the imaging kernel: image tile `tile` (8 columns, one per
+   warp), offset class `cls`, time window `win`.  nb counts the TMA batches
+   this CTA has issued (it selects the buffer and the mbarrier phase and
+   carries over between items).  Returns false if a bounded wait gave up. */
+template <int K, bool FULL, bool KAHAN, bool HILO>
+__device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem, int tile, int cls, int win,
+                                             uint32_t &nb)
 {
     constexpr int W = 32 * K;
     constexpr int TB = FULL ? KP_TB_FULL : KP_TB_REF;
-    extern __shared__ __align__(128) uint8_t smem[];
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    const int cls = blockIdx.y;
-    const int tw0 = blockIdx.z * W;
-    const int col = blockIdx.x * KPSTM_COLS_PER_CTA + w;
-    const bool colok = col < a.ncol;
+    const int tw0 = win * W;
+    const int col = a.tilecols[tile * KPSTM_COLS_PER_CTA + w]; /* -1: no column */
+    const bool colok = col >= 0;
     const int ns = a.ns;
     const int64_t row = a.row;
 
@@ -342,12 +409,12 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     int32_t *s_list = reinterpret_cast<int32_t *>(p);            /* [KP_LCH] */
     p += sizeof(int32_t) * KP_LCH;
     int32_t *s_wsum = reinterpret_cast<int32_t *>(p);            /* [8] */
-    p += sizeof(int32_t) * 8;
-    int32_t *s_flag = reinterpret_cast<int32_t *>(p);            /* [2]: abort, spare */
-    p += sizeof(int32_t) * 2;
-    p = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
-    uint64_t *s_bar = reinterpret_cast<uint64_t *>(p);           /* [2] */
+    /* flags end on an 8-byte boundary right before the barriers: the kernel
+       finds both at a.bar_offset (kp_image_smem computes the same layout) */
+    uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset); /* [2] */
+    int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2; /* [2]: abort, work item */
 
+    __syncthreads(); /* the previous item of this CTA is done with shared memory */
     const int vrow = colok ? a.colrow[col] : -1;
     const float rdt2 = a.rdt * a.rdt;
     if (FULL) {
@@ -371,16 +438,9 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
             reinterpret_cast<float2 *>(s_t)[i] = make_float2(ta < ns ? a.t2[ta] : 0.0f, tb < ns ? a.t2[tb] : 0.0f);
         }
     }
-    if (tid == 0) {
-        kp_mbar_init(&s_bar[0], 1);
-        kp_mbar_init(&s_bar[1], 1);
-        s_flag[0] = 0;
-        s_flag[1] = 0;
-        kp_fence_mbar_init();
-    }
     const float2 cxy = colok ? a.colxy[col] : make_float2(0.f, 0.f);
     const float IX = cxy.x, IY = cxy.y;
-    const float4 box = a.tilebox[blockIdx.x];
+    const float4 box = a.tilebox[tile];
     const int64_t obase = ((int64_t)cls * a.ncol + (colok ? col : 0)) * ns + tw0 + lane;
 
     /* accumulators as sample pairs: acc[q] = samples 2q (x) and 2q + 1 (y), i.e.
@@ -403,7 +463,6 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
 
     const int cb = a.class_start[cls], ce = a.class_start[cls + 1];
     const uint32_t row_bytes = (uint32_t)(row * sizeof(float));
-    uint32_t nb = 0; /* batches issued so far (buffer = nb & 1) */
     int my_hits = 0;
     bool abort = false;
     const float tmax = a.nsf - 1.0f;
@@ -576,7 +635,7 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
             }
         }
     }
-    if (abort) return;
+    if (abort) return false;
     if (colok) {
 #pragma unroll
         for (int q = 0; q < K / 2; ++q) {
@@ -593,7 +652,44 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
             }
         }
     }
-    if (blockIdx.z == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
+    if (win == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
+    return true;
+}
+
+/* Imaging kernel.  Grid mode (a.queue == null): one work item per CTA,
+   blockIdx = (tile, class, window).  Persistent mode: a grid sized to the
+   resident CTAs pulls items from a device counter; items are numbered class
+   by class in the order a.cls_order gives (largest classes first), so the
+   uneven class volumes of a batched launch finish together. */
+template <int K, bool FULL, bool KAHAN, bool HILO = false>
+__global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    /* barriers live at the end of the layout (see k_image_item) */
+    uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset);
+    int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2;
+    if (threadIdx.x == 0) {
+        kp_mbar_init(&s_bar[0], 1);
+        kp_mbar_init(&s_bar[1], 1);
+        s_flag[0] = 0;
+        s_flag[1] = 0;
+        kp_fence_mbar_init();
+    }
+    uint32_t nb = 0;
+    if (!a.queue) {
+        k_image_item<K, FULL, KAHAN, HILO>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, nb);
+        return;
+    }
+    const int per_class = a.ntile * a.nwin;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_flag[1] = atomicAdd(a.queue, 1);
+        __syncthreads();
+        const int item = s_flag[1];
+        if (item >= a.nitems) break;
+        const int r = item / per_class, rem = item - r * per_class;
+        if (!k_image_item<K, FULL, KAHAN, HILO>(a, smem, rem / a.nwin, a.cls_order[r], rem % a.nwin, nb)) break;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -603,39 +699,98 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
 struct KpDemigArgs {
     const kpstm_geom *geom;        /* live traces, slot order; geom.cls = class */
     const int32_t *nlive;
-    const float *model;            /* [ncol][ncls][ns] */
+    const float *model;            /* [ncol][ncls][ns]; null: the all-ones model (bound pass) */
     const float *tscale;           /* [ns] t / (8 dt) */
     const float2 *colxy;
     const int32_t *colrow;
     const float2 *vrows;           /* [nrow][ns] {v^2, RN(1/v^2)} */
     const float2 *t2c;             /* [ns] {(t/2)^2, .} */
+    const unsigned int *absmax;    /* bits of max |model| (k_absmax) */
+    const float *dbound;           /* [nlive] max_k (L 1)[trace, k] (bound pass), or null */
+    float *dbound_out;             /* bound pass: receives dbound */
     float *out;                    /* [ntr][ns] in block order */
+    unsigned long long *acc;       /* [nlive][ng] zeroed fixed-point accumulators (L2-resident rows) */
     int *status;
-    int nx, ny, ncls, ns;
+    int nx, ny, ncls, ns, ng;      /* ng: accumulator entries per trace, ns + tm - 1 */
+    int shift;                     /* bound pass: extra halvings of its scale (large images) */
     float ax0, adx, ay0, ady;      /* column coordinates: IX(xc) ~ ax0 + xc adx */
     double aperture;
-    float tmax, lmaxf, rdt2, aax, aay;
+    float tmax, lmaxf, rdt2, aax, aay, dt;
 };
 
-/* One warp per live trace: visits the image columns within the aperture of
-   the trace's midpoint (the same exact float test as k_image), computes every
-   pair with the same routines as k_image, and scatters
-   W max(0, Lf - |Tf - k|) into the trace (shared memory), W = weight x
-   t/(8 dt) x model - the exact transpose of k_image's
-   sum_k f[k] max(0, Lf - |Tf - k|). */
-__global__ void __launch_bounds__(256) k_demig(KpDemigArgs a)
+#define KP_DM_WARPS 4 /* traces (warps) per demigration CTA */
+
+/* Largest |x| as float bits (the order of non-negative floats is that of
+   their bits); NaN counts as infinity. */
+__global__ void __launch_bounds__(256) k_absmax(const float *x, int64_t n, unsigned int *out)
 {
-    extern __shared__ float dm_acc[];
+    unsigned int m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = fabsf(x[i]);
+        m = max(m, v == v ? __float_as_uint(v) : 0x7f800000u);
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+/* Demigration d = L m, the exact transpose of the full-mode migration of
+   k_image (HILO).  One warp per live trace visits the image columns within
+   the aperture of the trace's midpoint (the same exact float test as
+   k_image) and computes every pair with the same routines.  The migration
+   reads V(x) = (1 - f) P[n] + f P[n + 1] (n = floor(x), P the double running
+   integral, P[i] = sum_{k <= i} f[k] (i - k + 1)) at x0 = Tf - 1 (coefficient
+   -2) and x0 +- Lf (coefficient 1); the transpose adds c g (1 - f) at n and
+   c g f at n + 1, g = weight x t/(8 dt) x m - six entries per pair instead
+   of the 2 Lf + 1 of an explicit triangle - and the trace is
+   d[k] = sum_{i >= k} G[i] (i - k + 1), two reverse prefix sums.
+   Exactness: G is 64-bit fixed point, e1 = RN(c gs f), e0 = c Q - e1 with
+   Q = RN(gs), so each pair's entries sum to exactly zero and integer sums
+   carry no rounding into the prefix sums.  The per-trace scale 2^E keeps
+   |d| 2^E < 2^61 from |L m| <= max|m| (L 1) (L has non-negative
+   coefficients); (L 1) per trace comes from a bound pass of this kernel on
+   the all-ones model with the conservative scale |gs| < 2^30 (weight x
+   t/(8 dt) <= 2/dt).  The result is deterministic.
+   The entries are added with fire-and-forget 64-bit atomics (RED) into the
+   trace's row in global memory, which stays in L2 while the warp works on
+   it; the prefix sums run in shared memory. */
+__global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
+{
+    extern __shared__ __align__(16) unsigned long long dm_acc[]; /* [KP_DM_WARPS][ng], then floats */
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ns = a.ns;
-    const int nsp = (ns + 3) & ~3;
-    float *acc = dm_acc + w * nsp;
-    for (int k = lane; k < nsp; k += 32) acc[k] = 0.0f;
-    __syncwarp();
-    const int slot = blockIdx.x * 8 + w;
-    if (slot >= *a.nlive) return; /* warps are independent: no block barrier below */
+    const int ns = a.ns, ng = a.ng;
+    unsigned long long *A = dm_acc + (size_t)w * ng;
+    float *s_t2 = reinterpret_cast<float *>(dm_acc + (size_t)KP_DM_WARPS * ng); /* [ns] (t/2)^2 */
+    float *s_ts = s_t2 + ns;                                                    /* [ns] t/(8 dt) */
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+        s_t2[k] = a.t2c[k].x;
+        s_ts[k] = a.tscale[k];
+    }
+    __syncthreads();
+    const bool bound = a.model == nullptr;
+    const unsigned int mb = bound ? __float_as_uint(1.0f) : *a.absmax;
+    if (mb == 0u) return; /* zero model: the data stay zero */
+    if (mb >= 0x7f800000u) {
+        if (threadIdx.x == 0) kp_fail(a.status, KPSTM_ERR_INVALID_ARG); /* non-finite model */
+        return;
+    }
+    const int slot = blockIdx.x * KP_DM_WARPS + w;
+    if (slot >= *a.nlive) return; /* no block barrier below */
+    const float bw = 2.002f / a.dt; /* >= weight x t/(8 dt) over all pairs */
+    int E;
+    if (bound) {
+        E = 29 - (ilogbf(bw) + 1) - a.shift; /* |gs| < 2^30 */
+    } else {
+        /* 2^E max|m| max(2 (L 1), 2 bw) < 2^61 */
+        const float v = __uint_as_float(mb) * fmaxf(2.0f * a.dbound[slot], 2.0f * bw);
+        E = 61 - (ilogbf(fminf(v, 3.0e38f)) + 1);
+    }
+    E = max(-126, min(127, E));
+    const float scale = __int_as_float((E + 127) << 23);
+    const float inv = ldexpf(1.0f, -E);
+
     const kpstm_geom g = a.geom[slot];
     const int cls = g.cls;
+    unsigned long long *Gg = a.acc + (int64_t)slot * ng;
     const float apm = (float)a.aperture * 1.00001f + 1.0f; /* range margin; exact test below */
     const int x_lo = max(0, (int)floorf((g.cmpx - apm - a.ax0) / a.adx) - 1);
     const int x_hi = min(a.nx - 1, (int)ceilf((g.cmpx + apm - a.ax0) / a.adx) + 1);
@@ -664,32 +819,75 @@ __global__ void __launch_bounds__(256) k_demig(KpDemigArgs a)
             const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
             const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
             const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
-            const float *m = a.model + ((int64_t)col * a.ncls + cls) * ns;
+            const float *m = bound ? nullptr : a.model + ((int64_t)col * a.ncls + cls) * ns;
             const float2 *vr = a.vrows + (int64_t)vrow * ns;
-            for (int t0 = 0; t0 < ns; t0 += 32) {
-                const int t = t0 + lane;
-                if (t >= ns) continue;
-                const float mv = m[t];
-                if (mv == 0.0f) continue;
-                const float2 tv = make_float2(a.t2c[t].x, vr[t].y * a.rdt2);
-                float rs, rr;
-                const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
-                if (!(Tf < a.tmax)) continue;
-                float Lf, wgt;
-                kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                const float W = wgt * (a.tscale[t] * mv);
-                const int k0 = max(0, (int)floorf(Tf - Lf) + 1);
-                const int k1 = min(ns - 1, (int)ceilf(Tf + Lf) - 1);
-                for (int k = k0; k <= k1; ++k) {
-                    const float wk = Lf - fabsf(Tf - (float)k);
-                    if (wk > 0.0f) atomicAdd(&acc[k], W * wk);
+            for (int t = lane; t < ns; t += 32) {
+                {
+                const float mv = bound ? 1.0f : m[t];
+                if (mv != 0.0f) {
+                    const float2 tv = make_float2(s_t2[t], __fmul_rn(vr[t].y, a.rdt2)); /* as k_image's s_v */
+                    float rs, rr;
+                    const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
+                    if (Tf < a.tmax) {
+                        float Lf, wgt;
+                        kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
+                        const float gs = __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[t], mv)), scale);
+                        const long long Q = __float2ll_rn(gs);
+                        /* the positions exactly as k_image computes them */
+                        const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
+                        const int ba = kp_floor_bits(xa), bb = kp_floor_bits(xb), b00 = kp_floor_bits(x0);
+                        const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
+                        const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
+                        const float f0 = x0 - (__int_as_float(b00) - KP_MAGIC);
+                        /* n = floor(x); entries at n and n + 1, positions < 0 dropped */
+                        const int na = ba - KP_MAGIC_BITS, nb = bb - KP_MAGIC_BITS, n0 = b00 - KP_MAGIC_BITS;
+                        const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
+                        const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
+                        const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
+                        if (na >= 0) atomicAdd(&Gg[na], (unsigned long long)(Q - a1));
+                        if (na >= -1) atomicAdd(&Gg[na + 1], (unsigned long long)a1);
+                        if (nb >= 0) atomicAdd(&Gg[nb], (unsigned long long)(Q - b1));
+                        if (nb >= -1) atomicAdd(&Gg[nb + 1], (unsigned long long)b1);
+                        if (n0 >= 0) atomicAdd(&Gg[n0], (unsigned long long)(-2 * Q - c1));
+                        if (n0 >= -1) atomicAdd(&Gg[n0 + 1], (unsigned long long)c1);
+                    }
+                }
                 }
             }
         }
     }
+    /* order the row's atomics before the warp reads it back (past L1) */
+    __threadfence();
     __syncwarp();
-    float *o = a.out + (int64_t)g.src * ns;
-    for (int k = lane; k < ns; k += 32) o[k] = acc[k];
+    for (int k = lane; k < ng; k += 32) A[k] = __ldcg(&Gg[k]);
+    __syncwarp();
+    /* d = two reverse prefix sums of G, lane l owning entries [l C, l C + C) */
+    const int C = (ng + 31) >> 5;
+    const int lo = min(ng, lane * C), hi = min(ng, lo + C);
+    for (int pass = 0; pass < 2; ++pass) {
+        unsigned long long tot = 0ull;
+        for (int i = lo; i < hi; ++i) tot += A[i];
+        unsigned long long incl = tot; /* sum over lanes >= lane */
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long v = __shfl_down_sync(0xffffffffu, incl, d);
+            if (lane + d < 32) incl += v;
+        }
+        unsigned long long run = incl - tot;
+        for (int i = hi - 1; i >= lo; --i) {
+            run += A[i];
+            A[i] = run;
+        }
+        __syncwarp();
+    }
+    float dmax = 0.0f;
+    if (bound) {
+        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)A[k]) * inv));
+        dmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dmax)));
+        if (lane == 0) a.dbound_out[slot] = dmax;
+    } else {
+        float *o = a.out + (int64_t)g.src * ns;
+        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)A[k]), inv);
+    }
 }
 
 /* live slot -> geometry in slot order */

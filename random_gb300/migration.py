@@ -112,6 +112,26 @@ class Migration:
         capi.check("kpstm_profile_read", self._lib.kpstm_profile_read(self._h, C.byref(pr)))
         return {f: getattr(pr, f) for f, _ in capi.KpstmProfile._fields_}
 
+    # -- launch configuration of the imaging kernel ------------------------
+    def launch_config(self) -> dict:
+        cfg = capi.KpstmLaunch()
+        capi.check("kpstm_get_launch", self._lib.kpstm_get_launch(self._h, C.byref(cfg)))
+        return {f: getattr(cfg, f) for f, _ in capi.KpstmLaunch._fields_ if f != "reserved"}
+
+    def set_launch(self, tile_px: int = 0, samples_per_lane: int = 0, persistent: int = 0, graph: int = 0) -> None:
+        """Imaging work split (kpstm_set_launch); results are identical for every choice."""
+        cfg = capi.KpstmLaunch(tile_px=tile_px, samples_per_lane=samples_per_lane, persistent=persistent,
+                               graph=graph)
+        capi.check("kpstm_set_launch", self._lib.kpstm_set_launch(self._h, C.byref(cfg)))
+
+    def autotune(self, d_hdr_be: int, d_samples: int, ntr: int) -> tuple[dict, float]:
+        """kpstm_autotune on a device block; returns (chosen configuration, its block time in ms)."""
+        cfg = capi.KpstmLaunch()
+        ms = C.c_float()
+        capi.check("kpstm_autotune", self._lib.kpstm_autotune(self._h, d_hdr_be, d_samples, ntr, C.byref(cfg),
+                                                               C.byref(ms)))
+        return {f: getattr(cfg, f) for f, _ in capi.KpstmLaunch._fields_ if f != "reserved"}, ms.value
+
     # -- least-squares migration (device pointers) ----------------------------
     def lsm_geometry(self, headers: np.ndarray, headers_are_be: bool = False) -> None:
         hdr = np.ascontiguousarray(headers if headers_are_be else segy.headers_be(headers), dtype=np.int32)

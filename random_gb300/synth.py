@@ -340,3 +340,31 @@ def patch3d(ntr: int, **kw) -> Survey:
     s = m.survey
     s.samples = synthesize_numpy(m)
     return s
+
+
+def offset_bin_counts(nbins: int = 64, mean: float = 15000.0, lo: int = 2000, hi: int = 40000,
+                      seed: int = 4) -> np.ndarray:
+    """Traces per offset bin of the batched offset-class workload:
+    Poisson(mean) clipped to [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.clip(rng.poisson(mean, nbins), lo, hi).astype(np.int64)
+
+
+def offset_bins_model(counts, max_offset: float = 4000.0, ns: int = 1001, dt: float = 0.004,
+                      nx: int = 160, ny: int = 160, bin_m: float = 12.5, aperture: float = 1500.0,
+                      seed: int = 4, **kw) -> Patch3DModel:
+    """Batched offset-class survey: len(counts) offset bins of equal width
+    over [0, max_offset), bin b holding counts[b] traces with offsets uniform
+    inside it (random azimuths, midpoints uniform over the nx x ny patch),
+    imaged as offset gathers with one class per bin.  Traces are shuffled so
+    that every block mixes all bins."""
+    counts = np.asarray(counts, np.int64)
+    nb = len(counts)
+    dh = max_offset / nb
+    rng = np.random.default_rng(seed + 1000)
+    off = np.concatenate([rng.uniform(b * dh, (b + 1) * dh, int(n)) for b, n in enumerate(counts)])
+    off = off[rng.permutation(off.size)]
+    base = dict(ns=ns, dt=dt, nx=nx, ny=ny, bin_m=bin_m, max_offset=max_offset, aperture=aperture,
+                seed=seed, output=0, nh=nb, oh=0.0, dh=dh, offsets=off, name="offset_bins")
+    base.update(kw)
+    return patch3d_model(int(off.size), **base)
