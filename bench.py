@@ -239,7 +239,7 @@ def run_ours(args, rank, world, local_rank):
     launches = max(1, int(prof["image_launches"]))
     t_launch = prof["image_ms"] / 1e3 / launches
     row_floats = 2 * (NS + 2 * m.dims["trange_max"] - 2)
-    row_floats = (row_floats + 3) & ~3
+    row_floats = 8 + ((row_floats + 3) & ~3)  # geometry header + taps
     b_alg = algorithmic_bytes_per_step(model, block, row_floats)
     achieved = b_alg / t_launch / 1e9
     pairs_per_launch = pairs / launches

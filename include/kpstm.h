@@ -258,6 +258,9 @@ int kpstm_lsm_forward(kpstm_ctx *ctx, const float *d_model, float *d_data);
    as bf16 with a per-trace scale.  resid (nullable, niter + 1 values)
    receives ||d - L m_k||. */
 int kpstm_lsm_cg(kpstm_ctx *ctx, const float *d_data, int32_t niter, float *d_model, double *resid);
+/* Pairs (trace, in-aperture column, sample) of one operator application,
+   counted by the last kpstm_lsm_adjoint (L visits the same pairs). */
+int kpstm_lsm_pair_count(kpstm_ctx *ctx, int64_t *pairs);
 
 /* ---- finishing without device allocation ------------------------------------ */
 

@@ -154,6 +154,7 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_lsm_adjoint", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_lsm_forward", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_lsm_cg", C.c_int, [_VOIDP, _VOIDP, C.c_int32, _VOIDP, _VOIDP])
+    _sig(lib, "kpstm_lsm_pair_count", C.c_int, [_VOIDP, C.POINTER(i64)])
     _sig(lib, "kpstm_finish_noalloc", C.c_int, [C.POINTER(KpstmParams), _VOIDP, _VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_aliasfilter", C.c_int, [i32, C.c_float, C.c_double, C.c_double, C.c_double,
                                             C.POINTER(i32), _VOIDP])

@@ -145,6 +145,16 @@ static void prof_end(kpstm_ctx *c, int i, int stage, int launches)
 
 static int kp_free_all(kpstm_ctx *c);
 
+/* The float T with (x < T) == ((double)x < A) for every float x: the
+   reference compares a float distance with the double aperture
+   (Kirchhoff.c:1352-1354); the kernels make the same decision in fp32. */
+static float strict_bound_f(double A)
+{
+    const float f = (float)A;
+    if (A != A || (double)f >= A) return f; /* exact, or f is the next float above A */
+    return nextafterf(f, INFINITY);
+}
+
 /* ---- imaging launch ------------------------------------------------------- */
 
 static size_t image_smem_row(const kpstm_ctx *c, int64_t row, uint32_t *bar_offset)
@@ -545,9 +555,9 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             c->nsm = 1;
     }
     if (params->mode == KPSTM_MODE_FULL)
-        c->row = ((2 * (int64_t)(ns + 2 * tm - 2)) + 3) & ~int64_t(3); /* entries 0 .. ns + 2tm - 3 */
+        c->row = KP_ROW_HDR + (((2 * (int64_t)(ns + 2 * tm - 2)) + 3) & ~int64_t(3)); /* entries 0 .. ns + 2tm - 3 */
     else
-        c->row = (ns + 1 + 3) & ~3; /* D[0..ns-1] plus a zero sentinel D[ns] */
+        c->row = KP_ROW_HDR + ((ns + 1 + 3) & ~3); /* D[0..ns-1] plus a zero sentinel D[ns] */
 
     /* host tables */
     float *colxy = (float *)malloc(sizeof(float) * 2 * ncol);
@@ -1240,6 +1250,7 @@ static KpImageArgs image_args(const kpstm_ctx *c)
     a.rdt = 1.0f / p->dt;
     a.nsf = (float)p->ns;
     a.aperture = p->aperture;
+    a.aperture_f = strict_bound_f(p->aperture);
     float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
     a.tile_r2 = r * r;
     a.aax = (float)p->iline_distance;
@@ -1255,6 +1266,7 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
     KP_CUDA(cudaMemsetAsync(c->d_lkm, 0, sizeof(float) * nimg, c->cs));
     KP_CUDA(cudaMemsetAsync(c->d_lcnt, 0, sizeof(int32_t) * nimg, c->cs));
     if (c->d_lkc) KP_CUDA(cudaMemsetAsync(c->d_lkc, 0, sizeof(float) * nimg, c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_lhits, 0, sizeof(unsigned long long), c->cs));
     if (c->lsm_nlive > 0) {
         KpPrepArgs pa;
         memset(&pa, 0, sizeof(pa));
@@ -1323,6 +1335,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     if (a.adx == 0.0f) a.adx = 1.0f;
     if (a.ady == 0.0f) a.ady = 1.0f;
     a.aperture = p->aperture;
+    a.aperture_f = strict_bound_f(p->aperture);
     a.tmax = (float)ns - 1.0f;
     a.lmaxf = (float)s->lmax;
     const float rdt = 1.0f / p->dt;
@@ -1363,6 +1376,17 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     KP_CUDA(cudaGetLastError());
     k_demig<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(a);
     KP_CUDA(cudaGetLastError());
+    return KPSTM_OK;
+}
+
+extern "C" int kpstm_lsm_pair_count(kpstm_ctx *c, int64_t *pairs)
+{
+    if (!c || !pairs) return KPSTM_ERR_INVALID_ARG;
+    if (!c->d_lhits) return KPSTM_ERR_STATE;
+    unsigned long long h = 0;
+    KP_CUDA(cudaMemcpyAsync(&h, c->d_lhits, sizeof(h), cudaMemcpyDeviceToHost, c->cs));
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    *pairs = (int64_t)h * c->p.ns;
     return KPSTM_OK;
 }
 
@@ -1407,6 +1431,10 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         KP_LALLOC(c->d_lkm, sizeof(float) * nimg);
         KP_LALLOC(c->d_lcnt, sizeof(int32_t) * nimg);
         KP_LALLOC(c->d_lhits, sizeof(unsigned long long));
+        if (cudaMemsetAsync(c->d_lhits, 0, sizeof(unsigned long long), c->cs) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
         KP_LALLOC(c->d_dotpart, sizeof(double) * KP_DOT_BLOCKS);
         KP_LALLOC(c->d_dot, sizeof(double) * 4);
         KP_LALLOC(c->d_absmax, sizeof(unsigned int));
@@ -1451,7 +1479,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         }
         c->lsm_ntr = ntr;
         c->lsm_nlive = nl;
-        c->lrow = 4 * (int64_t)(ns + 2 * tm - 2);
+        c->lrow = KP_ROW_HDR + 4 * (int64_t)(ns + 2 * tm - 2);
         if (cudaMalloc(&c->d_ltable, sizeof(float) * c->lrow * (size_t)(nl > 0 ? nl : 1)) != cudaSuccess) {
             st = KPSTM_ERR_OUT_OF_MEMORY;
             break;

@@ -22,6 +22,7 @@
 #define KP_TB_FULL 2    /* traces per staged batch, full mode */
 #define KP_LCH 1024     /* traces examined per compaction chunk */
 #define KP_THREADS 256  /* 8 warps = KPSTM_COLS_PER_CTA columns */
+#define KP_ROW_HDR 8    /* floats of trace geometry at the start of every tap-table row */
 
 struct KpGeomArgs {
     const int32_t *hdr_be; /* [ntr][60] */
@@ -71,6 +72,7 @@ struct KpImageArgs {
     int ncol, ns, tm, lmax;
     float dt, rdt, nsf, lmaxf;
     double aperture;
+    float aperture_f;              /* float x: x < aperture_f exactly when (double)x < aperture */
     float tile_r2;                 /* squared tile-test radius (aperture + margin) */
     float aax, aay;                /* full mode: line spacings */
     const int32_t *tilecols;       /* [ntile][8] column of each warp, -1 = none */
@@ -238,7 +240,11 @@ __global__ void k_prep(KpPrepArgs a)
     kpstm_geom g = a.geom_raw[src];
     a.geom[i] = g;
     const int ns = a.ns, tm = a.tm;
-    float *row = a.table + i * a.row;
+    /* the row starts with the trace's geometry (staged with the taps) */
+    *reinterpret_cast<float4 *>(a.table + i * a.row) = make_float4(g.sxt, g.syt, g.gxt, g.gyt);
+    *reinterpret_cast<float4 *>(a.table + i * a.row + 4) =
+        make_float4(g.cmpx, g.cmpy, __int_as_float(g.cls), __int_as_float(g.src));
+    float *row = a.table + i * a.row + KP_ROW_HDR;
     const float *f32 = a.samples ? a.samples + (int64_t)src * ns : nullptr;
     const uint16_t *f16 = a.samples_bf16 ? a.samples_bf16 + (int64_t)src * ns : nullptr;
     const float sc = f16 ? a.scale[src] : 1.0f;
@@ -362,17 +368,19 @@ __device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float 
 }
 
 /* Shared-memory layout of k_image: s_v (8 warps x W float2), s_t (W
-   float2), two TMA buffers of TB rows, the compaction list, 8 warp counts,
-   2 flags and 2 mbarriers.  Returns the total bytes; *bar_offset receives
-   the barriers' offset (8-byte aligned, flags right before them). */
+   float2), S = 2 TB one-trace TMA stages, the compaction list, then 26 ints
+   (8 warp counts, 8 stage counters, 8 last-issued sequence numbers, 2 flags)
+   ending right before the S mbarriers.  Returns the total bytes;
+   *bar_offset receives the barriers' offset (8-byte aligned). */
+#define KP_IMG_INTS 26
 __host__ __device__ inline size_t kp_image_smem(int K, int TB, int64_t row, uint32_t *bar_offset)
 {
     const size_t W = 32 * (size_t)K;
     size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * 2 * TB * (size_t)row +
-               sizeof(int32_t) * (KP_LCH + 8);
-    b = ((b + 8 + 7) & ~size_t(7)); /* end of the two flags, 8-byte aligned */
+               sizeof(int32_t) * KP_LCH;
+    b = (b + sizeof(int32_t) * KP_IMG_INTS + 7) & ~size_t(7); /* end of the ints, 8-byte aligned */
     if (bar_offset) *bar_offset = (uint32_t)b;
-    return b + 2 * sizeof(uint64_t);
+    return b + 2 * TB * sizeof(uint64_t);
 }
 
 /* One work item of the imaging kernel: image tile `tile` (8 columns, one per
@@ -384,7 +392,7 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                              uint32_t &nb)
 {
     constexpr int W = 32 * K;
-    constexpr int TB = FULL ? KP_TB_FULL : KP_TB_REF;
+    constexpr int S = 2 * (FULL ? KP_TB_FULL : KP_TB_REF); /* one-trace pipeline stages */
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int tw0 = win * W;
     const int col = a.tilecols[tile * KPSTM_COLS_PER_CTA + w]; /* -1: no column */
@@ -404,15 +412,15 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     p += sizeof(float2) * KPSTM_COLS_PER_CTA * W;
     float *s_t = reinterpret_cast<float *>(p);
     p += sizeof(float2) * W;
-    float *s_buf = reinterpret_cast<float *>(p);                 /* [2][TB][row] */
-    p += sizeof(float) * 2 * TB * row;
-    int32_t *s_list = reinterpret_cast<int32_t *>(p);            /* [KP_LCH] */
-    p += sizeof(int32_t) * KP_LCH;
-    int32_t *s_wsum = reinterpret_cast<int32_t *>(p);            /* [8] */
-    /* flags end on an 8-byte boundary right before the barriers: the kernel
-       finds both at a.bar_offset (kp_image_smem computes the same layout) */
-    uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset); /* [2] */
-    int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2; /* [2]: abort, work item */
+    float *s_buf = reinterpret_cast<float *>(p);                 /* [S][row] */
+    int32_t *s_list = reinterpret_cast<int32_t *>(p + sizeof(float) * S * row); /* [KP_LCH] */
+    /* the ints end right before the barriers (kp_image_smem computes the same layout) */
+    uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset);     /* [S] stage full */
+    int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2;  /* [2]: abort, work item */
+    int32_t *s_last = s_flag - 8;                                            /* [S] last q issued per stage */
+    int32_t *s_cnt = s_last - 8;                                             /* [S] warps done with a stage */
+    int32_t *s_wsum = s_cnt - 8;                                             /* [8] */
+    volatile int32_t *vflag = s_flag;
 
     __syncthreads(); /* the previous item of this CTA is done with shared memory */
     const int vrow = colok ? a.colrow[col] : -1;
@@ -492,43 +500,54 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
             n += total;
             __syncthreads();
         }
-        const int nbatch = (n + TB - 1) / TB;
-        auto issue = [&](int b, uint32_t slot) {
-            int j0 = b * TB, j1 = min(n, j0 + TB);
-            uint64_t *bar = &s_bar[slot & 1];
+        /* per-warp pipeline of S one-trace stages: the prologue stages the
+           first S traces; the last warp to finish with a stage refills it with
+           the trace S positions later, so warps drift apart by up to S - 1
+           traces instead of meeting at a barrier after every batch */
+        auto issue = [&](int j, uint32_t q) {
+            const int slot = (int)(q % S);
+            uint64_t *bar = &s_bar[slot];
             kp_fence_proxy_async();
-            kp_mbar_expect_tx(bar, (uint32_t)(j1 - j0) * row_bytes);
-            for (int j = j0; j < j1; ++j)
-                kp_bulk_g2s(s_buf + ((slot & 1) * TB + (j - j0)) * row, a.table + (int64_t)s_list[j] * row,
-                            row_bytes, bar);
+            kp_mbar_expect_tx(bar, row_bytes);
+            kp_bulk_g2s(s_buf + slot * row, a.table + (int64_t)s_list[j] * row, row_bytes, bar);
+            s_last[slot] = (int32_t)q;
         };
-        if (tid == 0 && nbatch > 0) issue(0, nb);
-        for (int b = 0; b < nbatch; ++b, ++nb) {
-            const bool next = b + 1 < nbatch;
-            if (tid == 0 && next) issue(b + 1, nb + 1);
-            if (!kp_mbar_wait(&s_bar[nb & 1], (nb >> 1) & 1)) {
-                s_flag[0] = 1;
+        if (tid == 0)
+            for (int j = 0; j < min(n, S); ++j) issue(j, nb + (uint32_t)j);
+        for (int j = 0; j < n; ++j) {
+            const uint32_t q = nb + (uint32_t)j;
+            const int slot = (int)(q % S);
+            if (vflag[0]) break;
+            if (!kp_mbar_wait(&s_bar[slot], (q / S) & 1)) {
+                vflag[0] = 1;
                 kp_fail(a.status, KPSTM_ERR_TIMEOUT);
-                /* do not leave with our next copy still landing in shared memory */
-                if (tid == 0 && next) kp_mbar_wait(&s_bar[(nb + 1) & 1], ((nb + 1) >> 1) & 1);
+                break;
             }
-            if (s_flag[0] == 0 && colok) {
-                const int j0 = b * TB, j1 = min(n, j0 + TB);
-                for (int j = j0; j < j1; ++j) {
-                    const kpstm_geom g = a.geom[s_list[j]];
+            if (colok) {
+                do {
+                    const float *hdr = s_buf + slot * row; /* geometry, then taps */
+                    const float4 g0 = *reinterpret_cast<const float4 *>(hdr);
+                    const float2 g1 = *reinterpret_cast<const float2 *>(hdr + 4);
+                    kpstm_geom g;
+                    g.sxt = g0.x;
+                    g.syt = g0.y;
+                    g.gxt = g0.z;
+                    g.gyt = g0.w;
+                    g.cmpx = g1.x;
+                    g.cmpy = g1.y;
                     float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
                     float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-                    if (!((double)dIC < a.aperture)) continue; /* Kirchhoff.c:1352-1354, warp-uniform */
+                    if (!(dIC < a.aperture_f)) break; /* Kirchhoff.c:1352-1354, warp-uniform */
                     if (vrow < 0) {
                         kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
-                        continue;
+                        break;
                     }
                     ++my_hits;
                     float sx = __fsub_rn(IX, g.sxt), sy = __fsub_rn(IY, g.syt);
                     float gx = __fsub_rn(IX, g.gxt), gy = __fsub_rn(IY, g.gyt);
                     const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
                     const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
-                    const float *tab = s_buf + ((nb & 1) * TB + (j - j0)) * row;
+                    const float *tab = hdr + KP_ROW_HDR;
                     const float2 *sv = s_v + w * W + lane;
                     if (!FULL) {
                         const float4 *sv4 = reinterpret_cast<const float4 *>(s_v) + w * (K / 2) * 32 + lane;
@@ -626,16 +645,30 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                             }
                         }
                     }
+                } while (0);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block(); /* this warp's reads of the stage come first */
+                if (atomicAdd(&s_cnt[slot], 1) == KPSTM_COLS_PER_CTA - 1) {
+                    s_cnt[slot] = 0;
+                    __threadfence_block();
+                    if (j + S < n) issue(j + S, q + S);
                 }
             }
-            __syncthreads();
-            if (s_flag[0]) {
-                abort = true;
-                break;
-            }
         }
+        nb += (uint32_t)n;
+        __syncthreads();
+        if (vflag[0]) abort = true; /* the same for every thread after the barrier */
     }
-    if (abort) return false;
+    if (abort) {
+        /* leave no copy landing in shared memory: at most one phase per stage
+           is outstanding, the last one issued */
+        if (tid == 0)
+            for (int sl = 0; sl < S; ++sl)
+                if (s_last[sl] >= 0) kp_mbar_wait(&s_bar[sl], ((uint32_t)s_last[sl] / S) & 1);
+        return false;
+    }
     if (colok) {
 #pragma unroll
         for (int q = 0; q < K / 2; ++q) {
@@ -666,11 +699,15 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     /* barriers live at the end of the layout (see k_image_item) */
+    constexpr int S = 2 * (FULL ? KP_TB_FULL : KP_TB_REF);
     uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset);
     int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2;
     if (threadIdx.x == 0) {
-        kp_mbar_init(&s_bar[0], 1);
-        kp_mbar_init(&s_bar[1], 1);
+        for (int sl = 0; sl < S; ++sl) {
+            kp_mbar_init(&s_bar[sl], 1);
+            s_flag[-16 + sl] = 0;  /* stage counters */
+            s_flag[-8 + sl] = -1;  /* nothing issued yet */
+        }
         s_flag[0] = 0;
         s_flag[1] = 0;
         kp_fence_mbar_init();
@@ -715,10 +752,12 @@ struct KpDemigArgs {
     int shift;                     /* bound pass: extra halvings of its scale (large images) */
     float ax0, adx, ay0, ady;      /* column coordinates: IX(xc) ~ ax0 + xc adx */
     double aperture;
+    float aperture_f;              /* as KpImageArgs */
     float tmax, lmaxf, rdt2, aax, aay, dt;
 };
 
-#define KP_DM_WARPS 4 /* traces (warps) per demigration CTA */
+#define KP_DM_WARPS 4  /* traces (warps) per demigration CTA */
+#define KP_DM_UNROLL 4 /* 32-sample groups per load batch */
 
 /* Largest |x| as float bits (the order of non-negative floats is that of
    their bits); NaN counts as infinity. */
@@ -731,6 +770,13 @@ __global__ void __launch_bounds__(256) k_absmax(const float *x, int64_t n, unsig
     }
     m = __reduce_max_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+/* Fire-and-forget 64-bit add in global memory (RED: no value comes back, so
+   the warp does not wait for L2). */
+__device__ __forceinline__ void kp_red_add_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 /* Demigration d = L m, the exact transpose of the full-mode migration of
@@ -807,7 +853,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
             const float IX = cxy.x, IY = cxy.y;
             float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
             float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-            if (!((double)dIC < a.aperture)) continue;
+            if (!(dIC < a.aperture_f)) continue;
             const int vrow = a.colrow[col];
             if (vrow < 0) {
                 kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
@@ -821,37 +867,45 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
             const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
             const float *m = bound ? nullptr : a.model + ((int64_t)col * a.ncls + cls) * ns;
             const float2 *vr = a.vrows + (int64_t)vrow * ns;
-            for (int t = lane; t < ns; t += 32) {
-                {
-                const float mv = bound ? 1.0f : m[t];
-                if (mv != 0.0f) {
-                    const float2 tv = make_float2(s_t2[t], __fmul_rn(vr[t].y, a.rdt2)); /* as k_image's s_v */
+            /* 4 x 32 samples per step; their model and velocity loads (non-coherent,
+               so they can move ahead of the atomics) are all issued first */
+            for (int t0 = 0; t0 < ns; t0 += 32 * KP_DM_UNROLL) {
+                float mv[KP_DM_UNROLL], rv[KP_DM_UNROLL];
+#pragma unroll
+                for (int u = 0; u < KP_DM_UNROLL; ++u) {
+                    const int t = t0 + 32 * u + lane;
+                    mv[u] = t < ns ? (bound ? 1.0f : __ldg(m + t)) : 0.0f;
+                    rv[u] = t < ns ? __ldg(&vr[t].y) : 1.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < KP_DM_UNROLL; ++u) {
+                    const int t = t0 + 32 * u + lane;
+                    if (mv[u] == 0.0f) continue;
+                    const float2 tv = make_float2(s_t2[t], __fmul_rn(rv[u], a.rdt2)); /* as k_image's s_v */
                     float rs, rr;
                     const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
-                    if (Tf < a.tmax) {
-                        float Lf, wgt;
-                        kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                        const float gs = __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[t], mv)), scale);
-                        const long long Q = __float2ll_rn(gs);
-                        /* the positions exactly as k_image computes them */
-                        const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
-                        const int ba = kp_floor_bits(xa), bb = kp_floor_bits(xb), b00 = kp_floor_bits(x0);
-                        const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
-                        const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
-                        const float f0 = x0 - (__int_as_float(b00) - KP_MAGIC);
-                        /* n = floor(x); entries at n and n + 1, positions < 0 dropped */
-                        const int na = ba - KP_MAGIC_BITS, nb = bb - KP_MAGIC_BITS, n0 = b00 - KP_MAGIC_BITS;
-                        const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
-                        const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
-                        const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
-                        if (na >= 0) atomicAdd(&Gg[na], (unsigned long long)(Q - a1));
-                        if (na >= -1) atomicAdd(&Gg[na + 1], (unsigned long long)a1);
-                        if (nb >= 0) atomicAdd(&Gg[nb], (unsigned long long)(Q - b1));
-                        if (nb >= -1) atomicAdd(&Gg[nb + 1], (unsigned long long)b1);
-                        if (n0 >= 0) atomicAdd(&Gg[n0], (unsigned long long)(-2 * Q - c1));
-                        if (n0 >= -1) atomicAdd(&Gg[n0 + 1], (unsigned long long)c1);
-                    }
-                }
+                    if (!(Tf < a.tmax)) continue;
+                    float Lf, wgt;
+                    kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
+                    const float gs = __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[t], mv[u])), scale);
+                    const long long Q = __float2ll_rn(gs);
+                    /* the positions exactly as k_image computes them */
+                    const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
+                    const int ba = kp_floor_bits(xa), bb = kp_floor_bits(xb), b00 = kp_floor_bits(x0);
+                    const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
+                    const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
+                    const float f0 = x0 - (__int_as_float(b00) - KP_MAGIC);
+                    /* n = floor(x); entries at n and n + 1, positions < 0 dropped */
+                    const int na = ba - KP_MAGIC_BITS, nb = bb - KP_MAGIC_BITS, n0 = b00 - KP_MAGIC_BITS;
+                    const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
+                    const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
+                    const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
+                    if (na >= 0) kp_red_add_u64(&Gg[na], (unsigned long long)(Q - a1));
+                    if (na >= -1) kp_red_add_u64(&Gg[na + 1], (unsigned long long)a1);
+                    if (nb >= 0) kp_red_add_u64(&Gg[nb], (unsigned long long)(Q - b1));
+                    if (nb >= -1) kp_red_add_u64(&Gg[nb + 1], (unsigned long long)b1);
+                    if (n0 >= 0) kp_red_add_u64(&Gg[n0], (unsigned long long)(-2 * Q - c1));
+                    if (n0 >= -1) kp_red_add_u64(&Gg[n0 + 1], (unsigned long long)c1);
                 }
             }
         }

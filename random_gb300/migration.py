@@ -145,6 +145,12 @@ class Migration:
         """d_data = L d_model (demigration)."""
         capi.check("kpstm_lsm_forward", self._lib.kpstm_lsm_forward(self._h, d_model, d_data))
 
+    def lsm_pairs(self) -> int:
+        """Pairs of one operator application (counted by the last lsm_adjoint)."""
+        v = C.c_int64()
+        capi.check("kpstm_lsm_pair_count", self._lib.kpstm_lsm_pair_count(self._h, C.byref(v)))
+        return v.value
+
     def lsm_cg(self, d_data: int, niter: int, d_model: int) -> np.ndarray:
         resid = np.zeros(niter + 1, np.float64)
         capi.check("kpstm_lsm_cg", self._lib.kpstm_lsm_cg(self._h, d_data, niter, d_model, resid.ctypes.data))
