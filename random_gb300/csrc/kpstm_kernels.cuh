@@ -601,21 +601,25 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                         /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm;
                            the hi/lo table {hi(P(i)), lo(P(i)), P(i+1)-P(i), 0} keeps P to
                            ~1e-14 for noisy traces (least-squares operators) */
-                        const float2 *q2 = reinterpret_cast<const float2 *>(tab) + a.tm;
-                        const float4 *q4 = reinterpret_cast<const float4 *>(tab) + a.tm;
+                        /* the entry of P index floor(y) - 1 (x = y - 1 in the P index):
+                           q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm;
+                           the hi/lo table {hi(P(i)), lo(P(i)), P(i+1)-P(i), 0} keeps P to
+                           ~1e-14 for noisy traces (least-squares operators) */
+                        const float2 *q2 = reinterpret_cast<const float2 *>(tab) + (a.tm - 1);
+                        const float4 *q4 = reinterpret_cast<const float4 *>(tab) + (a.tm - 1);
 #pragma unroll
                         for (int k = 0; k < K; ++k) {
                             const float2 tv = sv[32 * k]; /* sample tw0 + lane + 32k */
                             float rs, rr;
                             const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
-                            if (Tf < tmax) { /* late samples of far traces skip the taps (whole warps) */
+                            if (Tf < tmax) { /* late samples of far traces skip the taps */
                                 float Lf, wgt;
                                 kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                                const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
-                                const int b0 = kp_floor_bits(x0), ba = kp_floor_bits(xa), bb = kp_floor_bits(xb);
-                                const float f0 = x0 - (__int_as_float(b0) - KP_MAGIC);
-                                const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
-                                const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
+                                const float y0 = Tf, ya = y0 + Lf, yb = y0 - Lf;
+                                const int b0 = kp_floor_bits(y0), ba = kp_floor_bits(ya), bb = kp_floor_bits(yb);
+                                const float f0 = y0 - (__int_as_float(b0) - KP_MAGIC);
+                                const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
+                                const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
                                 /* second difference without cancellation: table differences
                                    (exact for neighbouring values) plus the interpolation terms;
                                    equals sum_k f[k] max(0, Lf - |Tf - k|) */
@@ -635,9 +639,9 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 if (KAHAN) {
                                     float &ck = (k & 1) ? comp[k >> 1].y : comp[k >> 1].x;
                                     float y = fmaf(wgt, big + small, -ck);
-                                    float s = ak + y;
-                                    ck = (s - ak) - y;
-                                    ak = s;
+                                    float s2 = ak + y;
+                                    ck = (s2 - ak) - y;
+                                    ak = s2;
                                 } else {
                                     ak = fmaf(wgt, big + small, ak);
                                 }
@@ -779,6 +783,25 @@ __device__ __forceinline__ void kp_red_add_u64(unsigned long long *p, unsigned l
     asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+#define KP_DM_NONE (-(1 << 29)) /* entry index of a lane without a pair */
+
+/* One tap of the transpose for the 32 lanes of a warp (consecutive samples):
+   e0 at entry n, e1 at n + 1 (entries < 0 dropped).  Where the next lane's
+   n is this lane's n + 1 - the usual case, the traveltime advancing by about
+   a sample per sample - this lane's e1 is handed to it with a shuffle and
+   added to its e0, so one 64-bit RED per lane and tap reaches L2 instead of
+   two.  All lanes must call it. */
+__device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long long e0, long long e1, int lane)
+{
+    const int np = __shfl_up_sync(0xffffffffu, n, 1);
+    const long long e1p = __shfl_up_sync(0xffffffffu, e1, 1);
+    const int nn = __shfl_down_sync(0xffffffffu, n, 1);
+    if (lane > 0 && np + 1 == n) e0 += e1p;         /* the previous lane's e1 lands here */
+    const bool keep1 = !(lane < 31 && nn == n + 1); /* else the next lane takes it */
+    if (n >= 0) kp_red_add_u64(&G[n], (unsigned long long)e0);
+    if (keep1 && n >= -1) kp_red_add_u64(&G[n + 1], (unsigned long long)e1);
+}
+
 /* Demigration d = L m, the exact transpose of the full-mode migration of
    k_image (HILO).  One warp per live trace visits the image columns within
    the aperture of the trace's midpoint (the same exact float test as
@@ -879,33 +902,29 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                 }
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
-                    const int t = t0 + 32 * u + lane;
-                    if (mv[u] == 0.0f) continue;
-                    const float2 tv = make_float2(s_t2[t], __fmul_rn(rv[u], a.rdt2)); /* as k_image's s_v */
+                    const int t = t0 + 32 * u + lane, tt = min(t, ns - 1);
+                    const float2 tv = make_float2(s_t2[tt], __fmul_rn(rv[u], a.rdt2)); /* as k_image's s_v */
                     float rs, rr;
                     const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
-                    if (!(Tf < a.tmax)) continue;
+                    const bool ok = mv[u] != 0.0f && Tf < a.tmax;
+                    if (!__any_sync(0xffffffffu, ok)) continue; /* warp-uniform */
                     float Lf, wgt;
                     kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                    const float gs = __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[t], mv[u])), scale);
+                    const float gs = ok ? __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u])), scale) : 0.0f;
                     const long long Q = __float2ll_rn(gs);
-                    /* the positions exactly as k_image computes them */
-                    const float x0 = Tf - 1.0f, xa = x0 + Lf, xb = x0 - Lf;
-                    const int ba = kp_floor_bits(xa), bb = kp_floor_bits(xb), b00 = kp_floor_bits(x0);
-                    const float fa = xa - (__int_as_float(ba) - KP_MAGIC);
-                    const float fb = xb - (__int_as_float(bb) - KP_MAGIC);
-                    const float f0 = x0 - (__int_as_float(b00) - KP_MAGIC);
-                    /* n = floor(x); entries at n and n + 1, positions < 0 dropped */
-                    const int na = ba - KP_MAGIC_BITS, nb = bb - KP_MAGIC_BITS, n0 = b00 - KP_MAGIC_BITS;
+                    /* the positions exactly as k_image computes them: y = Tf, Tf +- Lf,
+                       P index n = floor(y) - 1, fraction y - floor(y) */
+                    const float y0 = ok ? Tf : 1.0f, ya = y0 + Lf, yb = y0 - Lf;
+                    const int ba = kp_floor_bits(ya), bb = kp_floor_bits(yb), b00 = kp_floor_bits(y0);
+                    const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
+                    const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
+                    const float f0 = y0 - (__int_as_float(b00) - KP_MAGIC);
                     const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
                     const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
                     const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
-                    if (na >= 0) kp_red_add_u64(&Gg[na], (unsigned long long)(Q - a1));
-                    if (na >= -1) kp_red_add_u64(&Gg[na + 1], (unsigned long long)a1);
-                    if (nb >= 0) kp_red_add_u64(&Gg[nb], (unsigned long long)(Q - b1));
-                    if (nb >= -1) kp_red_add_u64(&Gg[nb + 1], (unsigned long long)b1);
-                    if (n0 >= 0) kp_red_add_u64(&Gg[n0], (unsigned long long)(-2 * Q - c1));
-                    if (n0 >= -1) kp_red_add_u64(&Gg[n0 + 1], (unsigned long long)c1);
+                    kp_demig_tap(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
+                    kp_demig_tap(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
+                    kp_demig_tap(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
                 }
             }
         }

@@ -5,6 +5,7 @@ from __future__ import annotations
 
 import ctypes as C
 import re
+import subprocess
 from pathlib import Path
 
 import numpy as np
@@ -36,7 +37,7 @@ def test_library_exports_every_declared_symbol(kpstm_lib):
 
 def test_abi_version_and_strerror(kpstm_lib):
     assert kpstm_lib.kpstm_abi_version() == 1
-    for code in range(13):
+    for code in range(14):
         assert kpstm_lib.kpstm_strerror(code)
 
 
@@ -44,6 +45,29 @@ def test_struct_sizes_match_header_layout():
     # natural alignment of the C structs in include/kpstm.h
     assert C.sizeof(capi.KpstmParams) == 184
     assert C.sizeof(capi.KpstmDims) == 48
+
+
+def test_ctypes_layouts_match_the_c_compiler(tmp_path):
+    """Every ABI struct: sizeof and each field offset as gcc lays them out
+    from include/kpstm.h, against the ctypes mirror."""
+    structs = {"kpstm_params": capi.KpstmParams, "kpstm_velocity": capi.KpstmVelocity,
+               "kpstm_dims": capi.KpstmDims, "kpstm_profile": capi.KpstmProfile, "kpstm_launch": capi.KpstmLaunch}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "kpstm.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{HEADER.parent}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    for line in filter(None, out):
+        cname, what, val = line.split()
+        py = structs[cname]
+        want = C.sizeof(py) if what == "sizeof" else getattr(py, what).offset
+        assert int(val) == want, line
 
 
 def test_aliasfilter_matches_oracle(kpstm_lib, oracle_lib):
