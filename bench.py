@@ -370,7 +370,8 @@ def run_offset_bins(args):
             "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(elapsed / args.steps * 1e3, 3), "dtype": "bf16 store, f32 compute",
             "config": {"bins": 64, "traces": int(s.ntr), "traces_per_step": block, "ns": 1001,
-                       "image": "160x160x64x1001", "launch": cfg, "autotune_ms": round(tune_ms, 3)},
+                       "image": "160x160x64x1001", "autotuned": cfg, "launch": m.launch_config(),
+                       "autotune_ms": round(tune_ms, 3)},
             "pairs_per_step": pairs_timed / args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
 

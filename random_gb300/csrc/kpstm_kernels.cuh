@@ -623,27 +623,29 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 /* second difference without cancellation: table differences
                                    (exact for neighbouring values) plus the interpolation terms;
                                    equals sum_k f[k] max(0, Lf - |Tf - k|) */
-                                float big, small;
+                                float tri;
                                 if (HILO) {
                                     const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
                                     const float4 Qb = q4[bb - KP_MAGIC_BITS];
-                                    big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
-                                    small = fmaf(fa, Qa.z, fb * Qb.z) - 2.0f * (f0 * Q0.z);
+                                    const float big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
+                                    tri = fmaf(-2.0f * f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
                                 } else {
                                     const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
                                     const float2 Qb = q2[bb - KP_MAGIC_BITS];
-                                    big = (Qa.x - Q0.x) + (Qb.x - Q0.x);
-                                    small = fmaf(fa, Qa.y, fb * Qb.y) - 2.0f * (f0 * Q0.y);
+                                    /* each interpolation term joins the table difference of its own
+                                       tap (values of like size), the centre term last */
+                                    const float ua = fmaf(fa, Qa.y, Qa.x - Q0.x), ub = fmaf(fb, Qb.y, Qb.x - Q0.x);
+                                    tri = fmaf(-2.0f * f0, Q0.y, ua + ub);
                                 }
                                 float &ak = (k & 1) ? acc[k >> 1].y : acc[k >> 1].x;
                                 if (KAHAN) {
                                     float &ck = (k & 1) ? comp[k >> 1].y : comp[k >> 1].x;
-                                    float y = fmaf(wgt, big + small, -ck);
+                                    float y = fmaf(wgt, tri, -ck);
                                     float s2 = ak + y;
                                     ck = (s2 - ak) - y;
                                     ak = s2;
                                 } else {
-                                    ak = fmaf(wgt, big + small, ak);
+                                    ak = fmaf(wgt, tri, ak);
                                 }
                                 cnt[k] += 1;
                             }
@@ -774,6 +776,17 @@ __global__ void __launch_bounds__(256) k_absmax(const float *x, int64_t n, unsig
     }
     m = __reduce_max_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+/* RN(x) as a 64-bit integer for |x| < 2^62 without the float -> int64
+   conversion (which runs on the FP64 pipe, slow on GB300): x = h 2^31 + r with
+   h = trunc(x 2^-31) and r = x - h 2^31 exact (the low part of x's 24-bit
+   significand), then RN(x) = h 2^31 + RN(r) from two 32-bit conversions. */
+__device__ __forceinline__ long long kp_f2ll_rn(float x)
+{
+    const float hf = truncf(__fmul_rn(x, 4.656612873077392578125e-10f)); /* 2^-31, exact */
+    const float r = __fmaf_rn(-hf, 2147483648.0f, x);                   /* exact */
+    return ((long long)__float2int_rz(hf) << 31) + (long long)__float2int_rn(r);
 }
 
 /* Fire-and-forget 64-bit add in global memory (RED: no value comes back, so
@@ -911,7 +924,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                     float Lf, wgt;
                     kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
                     const float gs = ok ? __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u])), scale) : 0.0f;
-                    const long long Q = __float2ll_rn(gs);
+                    const long long Q = kp_f2ll_rn(gs);
                     /* the positions exactly as k_image computes them: y = Tf, Tf +- Lf,
                        P index n = floor(y) - 1, fraction y - floor(y) */
                     const float y0 = ok ? Tf : 1.0f, ya = y0 + Lf, yb = y0 - Lf;
@@ -919,9 +932,9 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                     const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
                     const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
                     const float f0 = y0 - (__int_as_float(b00) - KP_MAGIC);
-                    const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
-                    const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
-                    const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
+                    const long long a1 = kp_f2ll_rn(__fmul_rn(gs, fa));
+                    const long long b1 = kp_f2ll_rn(__fmul_rn(gs, fb));
+                    const long long c1 = kp_f2ll_rn(__fmul_rn(-2.0f * gs, f0));
                     kp_demig_tap(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
                     kp_demig_tap(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
                     kp_demig_tap(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
