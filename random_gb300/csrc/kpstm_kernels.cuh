@@ -778,17 +778,6 @@ __global__ void __launch_bounds__(256) k_absmax(const float *x, int64_t n, unsig
     if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
 }
 
-/* RN(x) as a 64-bit integer for |x| < 2^62 without the float -> int64
-   conversion (which runs on the FP64 pipe, slow on GB300): x = h 2^31 + r with
-   h = trunc(x 2^-31) and r = x - h 2^31 exact (the low part of x's 24-bit
-   significand), then RN(x) = h 2^31 + RN(r) from two 32-bit conversions. */
-__device__ __forceinline__ long long kp_f2ll_rn(float x)
-{
-    const float hf = truncf(__fmul_rn(x, 4.656612873077392578125e-10f)); /* 2^-31, exact */
-    const float r = __fmaf_rn(-hf, 2147483648.0f, x);                   /* exact */
-    return ((long long)__float2int_rz(hf) << 31) + (long long)__float2int_rn(r);
-}
-
 /* Fire-and-forget 64-bit add in global memory (RED: no value comes back, so
    the warp does not wait for L2). */
 __device__ __forceinline__ void kp_red_add_u64(unsigned long long *p, unsigned long long v)
@@ -924,7 +913,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                     float Lf, wgt;
                     kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
                     const float gs = ok ? __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u])), scale) : 0.0f;
-                    const long long Q = kp_f2ll_rn(gs);
+                    const long long Q = __float2ll_rn(gs);
                     /* the positions exactly as k_image computes them: y = Tf, Tf +- Lf,
                        P index n = floor(y) - 1, fraction y - floor(y) */
                     const float y0 = ok ? Tf : 1.0f, ya = y0 + Lf, yb = y0 - Lf;
@@ -932,9 +921,9 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                     const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
                     const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
                     const float f0 = y0 - (__int_as_float(b00) - KP_MAGIC);
-                    const long long a1 = kp_f2ll_rn(__fmul_rn(gs, fa));
-                    const long long b1 = kp_f2ll_rn(__fmul_rn(gs, fb));
-                    const long long c1 = kp_f2ll_rn(__fmul_rn(-2.0f * gs, f0));
+                    const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
+                    const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
+                    const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
                     kp_demig_tap(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
                     kp_demig_tap(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
                     kp_demig_tap(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
