@@ -243,13 +243,27 @@ def run_ours(args, rank, world, local_rank):
     b_alg = algorithmic_bytes_per_step(model, block, row_floats)
     achieved = b_alg / t_launch / 1e9
     pairs_per_launch = pairs / launches
+    # DRAM traffic per launch from ncu (dram__bytes_read + write) of a
+    # 5,000-trace launch of this kernel into the same image: 4.080e9 bytes, of
+    # which the tap tables are 5,000 rows; the accumulator part is fixed, the
+    # table part grows with the traces of the launch
+    traffic = 4.080e9 + (block - 5000) * row_floats * 4
+    # issue-slot roofline: warp instructions per pair from the same capture
+    # (55.2 per 32 pairs) against 4 schedulers x SMs x the SM clock
+    instr_per_pair = 55.2 / 32
+    issue_peak = 4 * 152 * (clk.get("sm_mhz") or peaks["sm_max_mhz"]) * 1e6
+    issue_achieved = pairs_per_launch / t_launch * instr_per_pair
     roofline = {
         "bound": "hbm", "achieved": round(achieved, 3), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": round(achieved / peaks["hbm_gbs"], 6), "traffic": None,
+        "frac": round(achieved / peaks["hbm_gbs"], 6), "traffic": round(traffic),
+        "traffic_source": "ncu dram bytes of a 5,000-trace launch, table part scaled to the block",
         "peak_source": peaks["source"], "kernel": "k_image (full mode)",
         "algorithmic_bytes_per_launch": b_alg, "launch_ms": round(t_launch * 1e3, 3),
         "pairs_per_launch": pairs_per_launch,
         "binding": "issue slots (no tensor work; HBM bytes per pair are ~1e-3): see profiles/",
+        "issue": {"achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
+                  "unit": "T warp-instr/s", "frac": round(issue_achieved / issue_peak, 4),
+                  "instr_per_pair_source": "ncu smsp__inst_executed / pairs, 5,000-trace launch"},
         "image_kernel_share": round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4),
     }
     del m
