@@ -97,6 +97,7 @@ struct kpstm_ctx {
     unsigned int *d_absmax;      /* demigration: bits of max |model| */
     float *d_dbound;             /* demigration: per live trace max_k (L 1)[k] */
     unsigned long long *d_dacc;  /* demigration: [nlive][ng] fixed-point trace accumulators */
+    int32_t *d_dorder;           /* demigration: live slots in Morton order of their midpoints */
     int dbound_ok;
     /* stream handling / profiling */
     cudaStream_t own_cs;
@@ -723,7 +724,7 @@ static int kp_free_all(kpstm_ctx *c)
                     c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
                     c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
                     c->d_lhits, c->d_dotpart, c->d_dot, c->d_smp16, c->d_scl16, c->d_tilecols, c->d_queue,
-                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc};
+                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
@@ -1349,6 +1350,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     const double cover = (double)s->ncol * ns * (s->lmax > 1 ? s->lmax : 1);
     a.shift = cover > 8589934592.0 ? (int)ceil(log2(cover / 8589934592.0)) : 0;
     a.absmax = c->d_absmax;
+    a.order = c->d_dorder;
     const size_t smem = sizeof(unsigned long long) * KP_DM_WARPS * (size_t)a.ng + sizeof(float) * 2 * (size_t)ns;
     if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
     const size_t accb = sizeof(unsigned long long) * (size_t)a.ng * (size_t)c->lsm_nlive;
@@ -1379,6 +1381,79 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     return KPSTM_OK;
 }
 
+/* The demigration's trace order: live slots sorted by a Morton (Z-order)
+   key of their midpoints on a grid of a quarter aperture, so that the warps
+   of a CTA, and CTAs running side by side, walk nearly the same image columns
+   and share their model and velocity rows in the caches.  (The migration
+   keeps class order; the result does not depend on this order.) */
+struct kp_zkey {
+    uint32_t key;
+    int32_t slot;
+};
+
+static int kp_zcmp(const void *a, const void *b)
+{
+    const kp_zkey *x = (const kp_zkey *)a, *y = (const kp_zkey *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->slot - y->slot;
+}
+
+static uint32_t kp_spread16(uint32_t v)
+{
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+static int spatial_order(kpstm_ctx *c, int32_t nl)
+{
+    cudaFree(c->d_dorder);
+    c->d_dorder = nullptr;
+    if (nl <= 0) return KPSTM_OK;
+    kpstm_geom *g = (kpstm_geom *)malloc(sizeof(kpstm_geom) * (size_t)nl);
+    kp_zkey *k = (kp_zkey *)malloc(sizeof(kp_zkey) * (size_t)nl);
+    int32_t *o = (int32_t *)malloc(sizeof(int32_t) * (size_t)nl);
+    int st = KPSTM_OK;
+    do {
+        if (!g || !k || !o) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        if (cudaMemcpy(g, c->d_lgeom, sizeof(kpstm_geom) * (size_t)nl, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            st = KPSTM_ERR_CUDA;
+            break;
+        }
+        float x0 = g[0].cmpx, y0 = g[0].cmpy;
+        for (int32_t i = 1; i < nl; ++i) {
+            x0 = fminf(x0, g[i].cmpx);
+            y0 = fminf(y0, g[i].cmpy);
+        }
+        const double cell = c->p.aperture > 0.0 ? 0.25 * c->p.aperture : 1.0;
+        for (int32_t i = 0; i < nl; ++i) {
+            double qx = floor((g[i].cmpx - x0) / cell), qy = floor((g[i].cmpy - y0) / cell);
+            qx = qx < 0.0 ? 0.0 : (qx > 65535.0 ? 65535.0 : qx);
+            qy = qy < 0.0 ? 0.0 : (qy > 65535.0 ? 65535.0 : qy);
+            k[i].key = kp_spread16((uint32_t)qx) | (kp_spread16((uint32_t)qy) << 1);
+            k[i].slot = i;
+        }
+        qsort(k, (size_t)nl, sizeof(kp_zkey), kp_zcmp);
+        for (int32_t i = 0; i < nl; ++i) o[i] = k[i].slot;
+        if (cudaMalloc(&c->d_dorder, sizeof(int32_t) * (size_t)nl) != cudaSuccess) {
+            st = KPSTM_ERR_OUT_OF_MEMORY;
+            break;
+        }
+        if (cudaMemcpy(c->d_dorder, o, sizeof(int32_t) * (size_t)nl, cudaMemcpyHostToDevice) != cudaSuccess)
+            st = KPSTM_ERR_CUDA;
+    } while (0);
+    free(g);
+    free(k);
+    free(o);
+    return st;
+}
+
 extern "C" int kpstm_lsm_pair_count(kpstm_ctx *c, int64_t *pairs)
 {
     if (!c || !pairs) return KPSTM_ERR_INVALID_ARG;
@@ -1397,11 +1472,12 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
     KP_CUDA(cudaStreamSynchronize(c->cs));
     void *old[] = {c->d_lgraw, c->d_lgeom, c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive,
                    c->d_lcnt, c->d_ltable, c->d_lkm, c->d_lhits, c->d_dotpart, c->d_dot, c->d_absmax,
-                   c->d_dbound, c->d_lkc, c->d_dacc};
+                   c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder};
     for (size_t i = 0; i < sizeof(old) / sizeof(old[0]); ++i)
         if (old[i]) cudaFree(old[i]);
     c->d_lkc = nullptr;
     c->d_dacc = nullptr;
+    c->d_dorder = nullptr;
     c->d_absmax = nullptr;
     c->d_dbound = nullptr;
     c->dbound_ok = 0;
@@ -1479,6 +1555,8 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         }
         c->lsm_ntr = ntr;
         c->lsm_nlive = nl;
+        st = spatial_order(c, nl);
+        if (st) break;
         c->lrow = KP_ROW_HDR + 4 * (int64_t)(ns + 2 * tm - 2);
         if (cudaMalloc(&c->d_ltable, sizeof(float) * c->lrow * (size_t)(nl > 0 ? nl : 1)) != cudaSuccess) {
             st = KPSTM_ERR_OUT_OF_MEMORY;

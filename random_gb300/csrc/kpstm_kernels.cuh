@@ -750,6 +750,7 @@ struct KpDemigArgs {
     const float2 *t2c;             /* [ns] {(t/2)^2, .} */
     const unsigned int *absmax;    /* bits of max |model| (k_absmax) */
     const float *dbound;           /* [nlive] max_k (L 1)[trace, k] (bound pass), or null */
+    const int32_t *order;          /* [nlive] visiting order of the live slots, or null */
     float *dbound_out;             /* bound pass: receives dbound */
     float *out;                    /* [ntr][ns] in block order */
     unsigned long long *acc;       /* [nlive][ng] zeroed fixed-point accumulators (L2-resident rows) */
@@ -844,8 +845,9 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
         if (threadIdx.x == 0) kp_fail(a.status, KPSTM_ERR_INVALID_ARG); /* non-finite model */
         return;
     }
-    const int slot = blockIdx.x * KP_DM_WARPS + w;
-    if (slot >= *a.nlive) return; /* no block barrier below */
+    const int wi = blockIdx.x * KP_DM_WARPS + w;
+    if (wi >= *a.nlive) return; /* no block barrier below */
+    const int slot = a.order ? a.order[wi] : wi;
     const float bw = 2.002f / a.dt; /* >= weight x t/(8 dt) over all pairs */
     int E;
     if (bound) {
