@@ -3,8 +3,11 @@
 properties that hold at any size, on a 10,000-trace block of the same
 survey (the FP64 oracle cannot run at this size):
 
-* linearity in the data: L^T(a d1 + d2) = a L^T d1 + L^T d2 up to the
-  rounding of fp32 sums over 10,000 traces (bar 3e-5 relative L2);
+* linearity in the data: L^T(a d1 + d2) = a L^T d1 + L^T d2 for two
+  band-limited datasets (the events of two seeded surveys on the same
+  geometry), up to the rounding of the fp32 tap tables and sums (bar 5e-5
+  relative L2; white noise would not do: its double running integral grows
+  like n^1.5 and the fp32 table of it loses ~1e-3 of the taps);
 * the pair count equals an independent count of the in-aperture
   (trace, column) pairs with the float32 test of Kirchhoff.c:1351-1354;
 * a block split is invisible: two 5,000-trace blocks give the same
@@ -24,11 +27,15 @@ torch = pytest.importorskip("torch")
 NTR = 10_000
 
 
+def _model(seed):
+    return synth.patch3d_model(1_000_000, ns=1501, dt=0.002, nx=400, ny=400, bin_m=25.0, max_offset=4000.0,
+                               n_refl=8, n_diff=200, freq=30.0, aperture=3000.0, aa_cutoff=100.0, seed=seed,
+                               mode=capi.MODE_FULL, output=capi.OUT_STACK, trace_slice=slice(0, NTR))
+
+
 @pytest.fixture(scope="module")
 def survey():
-    m = synth.patch3d_model(1_000_000, ns=1501, dt=0.002, nx=400, ny=400, bin_m=25.0, max_offset=4000.0,
-                            n_refl=8, n_diff=200, freq=30.0, aperture=3000.0, aa_cutoff=100.0, seed=2,
-                            mode=capi.MODE_FULL, output=capi.OUT_STACK, trace_slice=slice(0, NTR))
+    m = _model(2)
     d = synth.synthesize_torch(m, device="cuda")
     hdr = torch.from_numpy(np.ascontiguousarray(segy.headers_be(m.survey.headers), dtype=np.int32)).cuda()
     torch.cuda.synchronize()
@@ -47,15 +54,15 @@ def _accumulate(s, hdr, d, blocks):
 
 def test_linearity_in_the_data(kpstm_lib, survey):
     s, hdr, d1 = survey
-    g = torch.Generator(device="cuda")
-    g.manual_seed(5)
-    d2 = torch.randn(d1.shape, device="cuda", generator=g) * float(d1.std())
+    m2 = _model(7)  # other events; the same geometry (the trace draws come first)
+    m2.coords = _model(2).coords
+    d2 = synth.synthesize_torch(m2, device="cuda")
     a = 0.75
     k1, f1, p1 = _accumulate(s, hdr, d1.contiguous(), [NTR])
     k2, f2, _ = _accumulate(s, hdr, d2.contiguous(), [NTR])
     k3, f3, _ = _accumulate(s, hdr, (a * d1 + d2).contiguous(), [NTR])
     assert p1 > 0 and np.array_equal(f1, f2) and np.array_equal(f1, f3)
-    assert rel_l2(k3, a * k1.astype(np.float64) + k2) <= 3e-5
+    assert rel_l2(k3, a * k1.astype(np.float64) + k2) <= 5e-5
 
 
 def test_pair_count_is_exact(kpstm_lib, survey):
