@@ -98,6 +98,8 @@ struct kpstm_ctx {
     float *d_dbound;             /* demigration: per live trace max_k (L 1)[k] */
     unsigned long long *d_dacc;  /* demigration: [nlive][ng] fixed-point trace accumulators */
     int32_t *d_dorder;           /* demigration: live slots in Morton order of their midpoints */
+    float *d_rvdt;               /* demigration: [nrow][ns] 1/(v dt)^2 */
+    int nrow;                    /* velocity rows of the slab */
     int dbound_ok;
     /* stream handling / profiling */
     cudaStream_t own_cs;
@@ -652,6 +654,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             KP_ALLOC(c->d_queue, sizeof(int));
             KP_ALLOC(c->d_clsorder, sizeof(int32_t) * s.nclass);
             KP_ALLOC(c->d_vrows, sizeof(float2) * (size_t)(nrow > 0 ? nrow : 1) * ns);
+            c->nrow = nrow;
             KP_ALLOC(c->d_t2, sizeof(float) * ns);
             KP_ALLOC(c->d_t2c, sizeof(float2) * ns);
             if (params->mode == KPSTM_MODE_FULL) KP_ALLOC(c->d_tscale, sizeof(float) * ns);
@@ -724,7 +727,7 @@ static int kp_free_all(kpstm_ctx *c)
                     c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
                     c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
                     c->d_lhits, c->d_dotpart, c->d_dot, c->d_smp16, c->d_scl16, c->d_tilecols, c->d_queue,
-                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder};
+                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder, c->d_rvdt};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
@@ -1321,7 +1324,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.tscale = c->d_tscale;
     a.colxy = c->d_colxy;
     a.colrow = c->d_colrow;
-    a.vrows = c->d_vrows;
+    a.rvdt = c->d_rvdt;
     a.t2c = c->d_t2c;
     a.out = d_data;
     a.status = c->d_status;
@@ -1351,12 +1354,20 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.shift = cover > 8589934592.0 ? (int)ceil(log2(cover / 8589934592.0)) : 0;
     a.absmax = c->d_absmax;
     a.order = c->d_dorder;
-    const size_t smem = sizeof(unsigned long long) * KP_DM_WARPS * (size_t)a.ng + sizeof(float) * 2 * (size_t)ns;
+    const size_t smem = sizeof(float) * 2 * (size_t)ns;
     if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
     const size_t accb = sizeof(unsigned long long) * (size_t)a.ng * (size_t)c->lsm_nlive;
     if (!c->d_dacc) {
         if (cudaMalloc(&c->d_dacc, accb) != cudaSuccess) return KPSTM_ERR_OUT_OF_MEMORY;
     }
+    if (!c->d_rvdt) {
+        const int64_t nv = (int64_t)(c->nrow > 0 ? c->nrow : 1) * ns;
+        if (cudaMalloc(&c->d_rvdt, sizeof(float) * nv) != cudaSuccess) return KPSTM_ERR_OUT_OF_MEMORY;
+        const float rdt = 1.0f / p->dt;
+        k_rvdt<<<2 * c->nsm, 256, 0, c->cs>>>(c->d_vrows, nv, rdt * rdt, c->d_rvdt);
+        KP_CUDA(cudaGetLastError());
+    }
+    a.rvdt = c->d_rvdt;
     a.acc = c->d_dacc;
     KP_CUDA(cudaFuncSetAttribute(k_demig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned nblk = (unsigned)((c->lsm_nlive + KP_DM_WARPS - 1) / KP_DM_WARPS);

@@ -746,7 +746,7 @@ struct KpDemigArgs {
     const float *tscale;           /* [ns] t / (8 dt) */
     const float2 *colxy;
     const int32_t *colrow;
-    const float2 *vrows;           /* [nrow][ns] {v^2, RN(1/v^2)} */
+    const float *rvdt;             /* [nrow][ns] RN(RN(1/v^2) / dt^2): k_image's 1/(v dt)^2 */
     const float2 *t2c;             /* [ns] {(t/2)^2, .} */
     const unsigned int *absmax;    /* bits of max |model| (k_absmax) */
     const float *dbound;           /* [nlive] max_k (L 1)[trace, k] (bound pass), or null */
@@ -765,6 +765,13 @@ struct KpDemigArgs {
 
 #define KP_DM_WARPS 4  /* traces (warps) per demigration CTA */
 #define KP_DM_UNROLL 4 /* 32-sample groups per load batch */
+
+/* 1/(v dt)^2 per velocity-row sample, computed as k_image does it. */
+__global__ void k_rvdt(const float2 *vrows, int64_t n, float rdt2, float *out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __fmul_rn(vrows[i].y, rdt2);
+}
 
 /* Largest |x| as float bits (the order of non-negative floats is that of
    their bits); NaN counts as infinity. */
@@ -825,14 +832,13 @@ __device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long 
    The entries are added with fire-and-forget 64-bit atomics (RED) into the
    trace's row in global memory, which stays in L2 while the warp works on
    it; the prefix sums run in shared memory. */
-__global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
+__global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
 {
-    extern __shared__ __align__(16) unsigned long long dm_acc[]; /* [KP_DM_WARPS][ng], then floats */
+    extern __shared__ __align__(16) float dm_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ns = a.ns, ng = a.ng;
-    unsigned long long *A = dm_acc + (size_t)w * ng;
-    float *s_t2 = reinterpret_cast<float *>(dm_acc + (size_t)KP_DM_WARPS * ng); /* [ns] (t/2)^2 */
-    float *s_ts = s_t2 + ns;                                                    /* [ns] t/(8 dt) */
+    float *s_t2 = dm_smem;      /* [ns] (t/2)^2 */
+    float *s_ts = dm_smem + ns; /* [ns] t/(8 dt) */
     for (int k = threadIdx.x; k < ns; k += blockDim.x) {
         s_t2[k] = a.t2c[k].x;
         s_ts[k] = a.tscale[k];
@@ -893,7 +899,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
             const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
             const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
             const float *m = bound ? nullptr : a.model + ((int64_t)col * a.ncls + cls) * ns;
-            const float2 *vr = a.vrows + (int64_t)vrow * ns;
+            const float *vr = a.rvdt + (int64_t)vrow * ns;
             /* 4 x 32 samples per step; their model and velocity loads (non-coherent,
                so they can move ahead of the atomics) are all issued first */
             for (int t0 = 0; t0 < ns; t0 += 32 * KP_DM_UNROLL) {
@@ -902,12 +908,12 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
                     const int t = t0 + 32 * u + lane;
                     mv[u] = t < ns ? (bound ? 1.0f : __ldg(m + t)) : 0.0f;
-                    rv[u] = t < ns ? __ldg(&vr[t].y) : 1.0f;
+                    rv[u] = t < ns ? __ldg(vr + t) : 1.0f;
                 }
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
                     const int t = t0 + 32 * u + lane, tt = min(t, ns - 1);
-                    const float2 tv = make_float2(s_t2[tt], __fmul_rn(rv[u], a.rdt2)); /* as k_image's s_v */
+                    const float2 tv = make_float2(s_t2[tt], rv[u]); /* as k_image's s_v */
                     float rs, rr;
                     const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
                     const bool ok = mv[u] != 0.0f && Tf < a.tmax;
@@ -936,14 +942,13 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
     /* order the row's atomics before the warp reads it back (past L1) */
     __threadfence();
     __syncwarp();
-    for (int k = lane; k < ng; k += 32) A[k] = __ldcg(&Gg[k]);
-    __syncwarp();
-    /* d = two reverse prefix sums of G, lane l owning entries [l C, l C + C) */
+    /* d = two reverse prefix sums of G, in place in the row (L2), lane l owning
+       entries [l C, l C + C) */
     const int C = (ng + 31) >> 5;
     const int lo = min(ng, lane * C), hi = min(ng, lo + C);
     for (int pass = 0; pass < 2; ++pass) {
         unsigned long long tot = 0ull;
-        for (int i = lo; i < hi; ++i) tot += A[i];
+        for (int i = lo; i < hi; ++i) tot += __ldcg(&Gg[i]);
         unsigned long long incl = tot; /* sum over lanes >= lane */
         for (int d = 1; d < 32; d <<= 1) {
             const unsigned long long v = __shfl_down_sync(0xffffffffu, incl, d);
@@ -951,19 +956,19 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS) k_demig(KpDemigArgs a)
         }
         unsigned long long run = incl - tot;
         for (int i = hi - 1; i >= lo; --i) {
-            run += A[i];
-            A[i] = run;
+            run += __ldcg(&Gg[i]);
+            __stcg(&Gg[i], run);
         }
-        __syncwarp();
     }
+    __syncwarp(); /* the lanes' rows are visible to the whole warp */
     float dmax = 0.0f;
     if (bound) {
-        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)A[k]) * inv));
+        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)__ldcg(&Gg[k])) * inv));
         dmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dmax)));
         if (lane == 0) a.dbound_out[slot] = dmax;
     } else {
         float *o = a.out + (int64_t)g.src * ns;
-        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)A[k]), inv);
+        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)__ldcg(&Gg[k])), inv);
     }
 }
 
