@@ -392,6 +392,39 @@ def run_offset_bins(args):
     print(json.dumps(line), flush=True)
 
 
+def run_line(args):
+    """The 2-D line: 200 CMPs x 48 offsets = 9,600 traces, 1001 samples at
+    4 ms, 48 offset classes x 200 columns, reference operator (bit-exact
+    accumulators).  A step images the whole line once (1.61e9 pairs) from
+    device-resident traces."""
+    import torch
+    from random_gb300 import build, segy, synth
+    from random_gb300.migration import Migration
+    build.build()
+    dev = torch.device("cuda", 0)
+    s = synth.line2d()
+    d_hdr = torch.from_numpy(np.ascontiguousarray(segy.headers_be(s.headers))).to(dev)
+    d_smp = torch.from_numpy(np.ascontiguousarray(s.samples)).to(dev)
+    m = Migration(s.params, s.velocity)
+    stream = torch.cuda.Stream(device=dev)
+    m.set_stream(stream.cuda_stream)
+
+    def step(i):
+        m.add_traces_device(d_hdr.data_ptr(), d_smp.data_ptr(), s.ntr)
+
+    mark = {}
+    elapsed, clk = _timed_steps(step, args.warmup, args.steps, stream,
+                                after_warmup=lambda: mark.setdefault("p0", m.pairs()))
+    m.synchronize()
+    pairs = m.pairs() - mark["p0"]
+    line = {"workload": "line", "metric": METRIC, "value": round(pairs / elapsed / 1e9, 4), "unit": UNIT,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3),
+            "dtype": "f32", "config": {"traces": int(s.ntr), "ns": 1001, "image": "200x1x48x1001",
+                                       "mode": "reference (bit-exact)"},
+            "pairs_per_step": pairs / args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_lsm(args):
     """Least-squares operator pair on 250,000 traces (ns = 751 at 4 ms,
     offsets U(0, 3000 m), random azimuths) and a 200 x 200 x 751 model at
@@ -442,6 +475,21 @@ def run_lsm(args):
             "pairs_per_application": pairs_app,
             "config": {"traces": ntr, "ns": 751, "model": "200x200x751", "aperture_m": 3000.0},
             "clocks": clk}
+    if args.cg_iters > 0:
+        # least-squares migration of the survey's own events (bf16 data vectors,
+        # FP64 CG scalars): time and residual history of --cg-iters iterations
+        from random_gb300 import synth as _s
+        d_obs = _s.synthesize_torch(mdl, device=dev)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        resid = m.lsm_cg(d_obs.data_ptr(), args.cg_iters, model.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        secs = e0.elapsed_time(e1) / 1e3
+        line["cg"] = {"iterations": args.cg_iters, "seconds": round(secs, 3),
+                      "applications": 2 * args.cg_iters + 1,
+                      "residual_rel": [round(float(r / resid[0]), 6) for r in resid]}
     print(json.dumps(line), flush=True)
 
 
@@ -486,10 +534,11 @@ def main():
     ap.add_argument("--ref-traces", type=int, default=1500)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cg-iters", type=int, default=0, help="lsm workload: also time this many CG iterations")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
                     help="trace storage of the survey workload (bf16: per-trace scale, Kahan sums)")
-    ap.add_argument("--workload", choices=["survey", "offset-bins", "lsm"], default="survey",
-                    help="survey: the bench line; offset-bins / lsm: further measurements (1 GPU)")
+    ap.add_argument("--workload", choices=["survey", "offset-bins", "lsm", "line"], default="survey",
+                    help="survey: the bench line; offset-bins / lsm / line: further measurements (1 GPU)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -502,6 +551,9 @@ def main():
         return
     if args.workload == "lsm":
         run_lsm(args)
+        return
+    if args.workload == "line":
+        run_line(args)
         return
     if world > 1:
         import torch
