@@ -204,6 +204,11 @@ def run_ours(args, rank, world, local_rank):
     stream = torch.cuda.Stream(device=dev)
     m.set_stream(stream.cuda_stream)
 
+    tuned = None
+    if args.autotune > 0:
+        cfg, tune_ms = m.autotune(d_hdr.data_ptr(), d_smp.data_ptr(), args.autotune)
+        tuned = dict(cfg, sample_traces=args.autotune, block_ms=round(tune_ms, 3))
+
     def step(i):
         b = i % nblocks
         m.add_traces_device(d_hdr.data_ptr() + b * block * 240, d_smp.data_ptr() + b * block * row_bytes, block)
@@ -232,6 +237,7 @@ def run_ours(args, rank, world, local_rank):
     elapsed = e0.elapsed_time(e1) / 1e3
     prof = m.profile_read()
     m.profile(False)
+    launch_cfg = m.launch_config()
     pairs = m.pairs() - pairs0
     elapsed_max, pairs_all = multirank.reduce_timing(elapsed, float(pairs), device=dev)
     value = pairs_all / elapsed_max / 1e9
@@ -276,6 +282,7 @@ def run_ours(args, rank, world, local_rank):
         h_hdr = torch.from_numpy(hdr_be[:nb * block]).pin_memory()
         h_smp = d_smp[:nb * block].cpu().pin_memory()
         m2 = Migration(prm, s.velocity)
+        m2.set_launch(**launch_cfg)
         out = torch.empty((NX, NY, 1, NS), dtype=torch.float32).pin_memory()
         # one untimed block to create the staging buffers
         m2.add_traces_ptr(h_hdr.data_ptr(), h_smp.data_ptr(), block)
@@ -317,7 +324,7 @@ def run_ours(args, rank, world, local_rank):
                                    "25 m, aperture 3000 m, triangle anti-alias + spreading/obliquity, fp32",
                        "traces_per_step": block, "survey_traces": ntr, "mode": "full",
                        "l2": "inputs larger than L2: 613 MB tap tables + 1.9 GB image accumulators per step",
-                       "parallelism": f"image slabs x{world}"},
+                       "parallelism": f"image slabs x{world}", "launch": launch_cfg, "autotuned": tuned},
             "gpu_launches": int(prof["image_launches"] + prof["other_launches"]),
             "pairs": int(pairs_all), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "profile_ms": {"image": round(prof["image_ms"], 3), "prep": round(prof["prep_ms"], 3)},
@@ -535,6 +542,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cg-iters", type=int, default=0, help="lsm workload: also time this many CG iterations")
+    ap.add_argument("--autotune", type=int, default=0,
+                    help="survey workload: autotune the launch on this many traces before timing (0: default launch)")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
                     help="trace storage of the survey workload (bf16: per-trace scale, Kahan sums)")
     ap.add_argument("--workload", choices=["survey", "offset-bins", "lsm", "line"], default="survey",

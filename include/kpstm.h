@@ -220,14 +220,19 @@ typedef struct {
                              tap tables, imaging) is captured once per block shape
                              into a CUDA graph and replayed; ignored while
                              profiling is enabled */
-    int reserved[4];
+    int ctas_per_sm;      /* imaging kernel variant: 2 (default; 0 = 2) or 3 resident
+                             CTAs per SM - 3 trades register space (80 per thread, so
+                             samples_per_lane <= 16) and pipeline depth for 24
+                             resident warps; full mode with fp32 storage only */
+    int reserved[3];
 } kpstm_launch;
 int kpstm_get_launch(const kpstm_ctx *ctx, kpstm_launch *cfg);
 /* KPSTM_ERR_INVALID_ARG for a value outside the lists above. */
 int kpstm_set_launch(kpstm_ctx *ctx, const kpstm_launch *cfg);
 /* Autotuner: images the given device block (the layout of
    kpstm_add_traces_device) once per candidate configuration (tile_px x
-   samples_per_lane x persistent; the caller's graph flag is kept), times the
+   samples_per_lane x persistent x ctas_per_sm; the caller's graph flag is
+   kept), times the
    imaging kernel with CUDA events, selects the fastest, clears the image
    accumulators again and returns the choice in *best (nullable) and its time
    in *best_ms (nullable).  Only on a context without traces since

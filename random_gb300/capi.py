@@ -62,7 +62,7 @@ class KpstmProfile(C.Structure):
 
 class KpstmLaunch(C.Structure):
     _fields_ = [("tile_px", C.c_int32), ("samples_per_lane", C.c_int32), ("persistent", C.c_int32),
-                ("graph", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("graph", C.c_int32), ("ctas_per_sm", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class KpstmDims(C.Structure):

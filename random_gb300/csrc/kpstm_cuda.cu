@@ -46,6 +46,7 @@ struct kpstm_ctx {
     int64_t ntile;               /* image tiles of 8 columns */
     int tile_px;                 /* tile patch: tile_px x (8 / tile_px) columns */
     int persistent, use_graph;   /* launch configuration (kpstm_launch) */
+    int minb;                    /* imaging CTAs per SM the kernel variant is built for: 2 or 3 */
     int dirty;                   /* traces imaged since create / reset */
     int nsm;                     /* multiprocessors of the device */
     int64_t row;                 /* floats per tap-table row */
@@ -160,16 +161,15 @@ static float strict_bound_f(double A)
 
 /* ---- imaging launch ------------------------------------------------------- */
 
-static size_t image_smem_row(const kpstm_ctx *c, int64_t row, uint32_t *bar_offset)
+static size_t image_smem_row(const kpstm_ctx *c, int64_t row, bool hilo, uint32_t *bar_offset)
 {
-    const int TB = c->p.mode == KPSTM_MODE_FULL ? KP_TB_FULL : KP_TB_REF;
-    return kp_image_smem(c->K, TB, row, bar_offset);
+    return kp_image_smem(c->K, kp_stages(c->p.mode == KPSTM_MODE_FULL, hilo ? 2 : c->minb), row, bar_offset);
 }
 
 typedef void (*kp_image_fn)(KpImageArgs);
 
 template <int K>
-static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo)
+static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo, int minb)
 {
     if (hilo) {
         if constexpr (K <= 16) {
@@ -184,6 +184,10 @@ static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo)
         if constexpr (K <= 16) return full ? k_image<K, true, true> : k_image<K, false, true>;
         return nullptr;
     }
+    if (full && minb == 3) {
+        if constexpr (K <= 16) return k_image<K, true, false, false, 3>;
+        return nullptr;
+    }
     if (full) {
         if constexpr (K <= 24) return k_image<K, true, false>;
         return nullptr;
@@ -195,11 +199,12 @@ static kp_image_fn image_fn(const kpstm_ctx *c, bool hilo)
 {
     const bool full = c->p.mode == KPSTM_MODE_FULL;
     const bool kahan = c->p.precision == KPSTM_PREC_BF16_KAHAN;
+    const int minb = hilo ? 2 : c->minb;
     switch (c->K) {
-    case 8: return image_fn_k<8>(full, kahan, hilo);
-    case 16: return image_fn_k<16>(full, kahan, hilo);
-    case 24: return image_fn_k<24>(full, kahan, hilo);
-    default: return image_fn_k<32>(full, kahan, hilo);
+    case 8: return image_fn_k<8>(full, kahan, hilo, minb);
+    case 16: return image_fn_k<16>(full, kahan, hilo, minb);
+    case 24: return image_fn_k<24>(full, kahan, hilo, minb);
+    default: return image_fn_k<32>(full, kahan, hilo, minb);
     }
 }
 
@@ -211,7 +216,7 @@ static cudaError_t launch_image(kpstm_ctx *c, KpImageArgs a, int nclass, bool hi
 {
     kp_image_fn fn = image_fn(c, hilo);
     if (!fn) return cudaErrorInvalidValue;
-    size_t smem = image_smem_row(c, a.row, &a.bar_offset);
+    size_t smem = image_smem_row(c, a.row, hilo, &a.bar_offset);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     a.ntile = c->ntile;
@@ -551,6 +556,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     const int ns = params->ns, tm = s.dims.trange_max;
     const int ncol = s.ncol;
     set_K(c, default_K(params));
+    c->minb = 2;
     {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -1027,6 +1033,7 @@ extern "C" int kpstm_get_launch(const kpstm_ctx *c, kpstm_launch *cfg)
     cfg->samples_per_lane = c->K;
     cfg->persistent = c->persistent;
     cfg->graph = c->use_graph;
+    cfg->ctas_per_sm = c->minb;
     return KPSTM_OK;
 }
 
@@ -1039,9 +1046,14 @@ extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
 {
     if (!c || !cfg) return KPSTM_ERR_INVALID_ARG;
     const int px = cfg->tile_px ? cfg->tile_px : default_px(&c->s);
-    const int K = cfg->samples_per_lane ? cfg->samples_per_lane : default_K(&c->p);
+    const int minb = cfg->ctas_per_sm ? cfg->ctas_per_sm : 2;
+    int K = cfg->samples_per_lane ? cfg->samples_per_lane : default_K(&c->p);
+    if (minb == 3 && !cfg->samples_per_lane && K > 16) K = 16;
     if ((px != 1 && px != 2 && px != 4 && px != 8) || !valid_K(c, K)) return KPSTM_ERR_INVALID_ARG;
     if ((cfg->persistent != 0 && cfg->persistent != 1) || (cfg->graph != 0 && cfg->graph != 1))
+        return KPSTM_ERR_INVALID_ARG;
+    if (minb != 2 && minb != 3) return KPSTM_ERR_INVALID_ARG;
+    if (minb == 3 && !(c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32 && K <= 16))
         return KPSTM_ERR_INVALID_ARG;
     drop_graphs(c);
     if (px != c->tile_px) {
@@ -1049,6 +1061,7 @@ extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
         if (st) return st;
     }
     set_K(c, K);
+    c->minb = minb;
     c->persistent = cfg->persistent;
     c->use_graph = cfg->graph;
     return KPSTM_OK;
@@ -1081,12 +1094,16 @@ extern "C" int kpstm_autotune(kpstm_ctx *c, const int32_t *d_hdr_be, const float
         if (n > 2 * nmin) continue;
         for (int K = 8; K <= 32 && !st; K += 8) {
             if (!valid_K(c, K)) continue;
-            for (int pers = 0; pers <= 1 && !st; ++pers) {
+            for (int v = 0; v < 4 && !st; ++v) {
+                const int pers = v & 1, minb = 2 + (v >> 1);
+                if (minb == 3 && !(c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32 && K <= 16))
+                    continue;
                 kpstm_launch cfg;
                 memset(&cfg, 0, sizeof(cfg));
                 cfg.tile_px = px;
                 cfg.samples_per_lane = K;
                 cfg.persistent = pers;
+                cfg.ctas_per_sm = minb;
                 st = kpstm_set_launch(c, &cfg);
                 if (st) break;
                 float ms = 0.0f;

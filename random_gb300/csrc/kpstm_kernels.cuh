@@ -368,31 +368,37 @@ __device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float 
 }
 
 /* Shared-memory layout of k_image: s_v (8 warps x W float2), s_t (W
-   float2), S = 2 TB one-trace TMA stages, the compaction list, then 26 ints
+   float2), S one-trace TMA stages (kp_stages), the compaction list, then 26 ints
    (8 warp counts, 8 stage counters, 8 last-issued sequence numbers, 2 flags)
    ending right before the S mbarriers.  Returns the total bytes;
    *bar_offset receives the barriers' offset (8-byte aligned). */
 #define KP_IMG_INTS 26
-__host__ __device__ inline size_t kp_image_smem(int K, int TB, int64_t row, uint32_t *bar_offset)
+/* TMA stages of the imaging kernel: 2 x the batch of the mode, or 2 for the
+   three-CTAs-per-SM variant (MINB 3), whose shared memory must fit 3 times */
+__host__ __device__ constexpr int kp_stages(bool full, int minb)
+{
+    return minb >= 3 ? 2 : 2 * (full ? KP_TB_FULL : KP_TB_REF);
+}
+__host__ __device__ inline size_t kp_image_smem(int K, int S, int64_t row, uint32_t *bar_offset)
 {
     const size_t W = 32 * (size_t)K;
-    size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * 2 * TB * (size_t)row +
+    size_t b = sizeof(float2) * KPSTM_COLS_PER_CTA * W + sizeof(float2) * W + sizeof(float) * S * (size_t)row +
                sizeof(int32_t) * KP_LCH;
     b = (b + sizeof(int32_t) * KP_IMG_INTS + 7) & ~size_t(7); /* end of the ints, 8-byte aligned */
     if (bar_offset) *bar_offset = (uint32_t)b;
-    return b + 2 * TB * sizeof(uint64_t);
+    return b + S * sizeof(uint64_t);
 }
 
 /* One work item of the imaging kernel: image tile `tile` (8 columns, one per
    warp), offset class `cls`, time window `win`.  nb counts the TMA batches
    this CTA has issued (it selects the buffer and the mbarrier phase and
    carries over between items).  Returns false if a bounded wait gave up. */
-template <int K, bool FULL, bool KAHAN, bool HILO>
+template <int K, bool FULL, bool KAHAN, bool HILO, int MINB>
 __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem, int tile, int cls, int win,
                                              uint32_t &nb)
 {
     constexpr int W = 32 * K;
-    constexpr int S = 2 * (FULL ? KP_TB_FULL : KP_TB_REF); /* one-trace pipeline stages */
+    constexpr int S = kp_stages(FULL, MINB); /* one-trace pipeline stages */
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int tw0 = win * W;
     const int col = a.tilecols[tile * KPSTM_COLS_PER_CTA + w]; /* -1: no column */
@@ -700,12 +706,12 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
    resident CTAs pulls items from a device counter; items are numbered class
    by class in the order a.cls_order gives (largest classes first), so the
    uneven class volumes of a batched launch finish together. */
-template <int K, bool FULL, bool KAHAN, bool HILO = false>
-__global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
+template <int K, bool FULL, bool KAHAN, bool HILO = false, int MINB = 2>
+__global__ void __launch_bounds__(KP_THREADS, MINB) k_image(KpImageArgs a)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     /* barriers live at the end of the layout (see k_image_item) */
-    constexpr int S = 2 * (FULL ? KP_TB_FULL : KP_TB_REF);
+    constexpr int S = kp_stages(FULL, MINB);
     uint64_t *s_bar = reinterpret_cast<uint64_t *>(smem + a.bar_offset);
     int32_t *s_flag = reinterpret_cast<int32_t *>(smem + a.bar_offset) - 2;
     if (threadIdx.x == 0) {
@@ -720,7 +726,7 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
     }
     uint32_t nb = 0;
     if (!a.queue) {
-        k_image_item<K, FULL, KAHAN, HILO>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, nb);
+        k_image_item<K, FULL, KAHAN, HILO, MINB>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, nb);
         return;
     }
     const int per_class = a.ntile * a.nwin;
@@ -731,7 +737,7 @@ __global__ void __launch_bounds__(KP_THREADS, 2) k_image(KpImageArgs a)
         const int item = s_flag[1];
         if (item >= a.nitems) break;
         const int r = item / per_class, rem = item - r * per_class;
-        if (!k_image_item<K, FULL, KAHAN, HILO>(a, smem, rem / a.nwin, a.cls_order[r], rem % a.nwin, nb)) break;
+        if (!k_image_item<K, FULL, KAHAN, HILO, MINB>(a, smem, rem / a.nwin, a.cls_order[r], rem % a.nwin, nb)) break;
     }
 }
 

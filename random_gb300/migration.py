@@ -118,10 +118,11 @@ class Migration:
         capi.check("kpstm_get_launch", self._lib.kpstm_get_launch(self._h, C.byref(cfg)))
         return {f: getattr(cfg, f) for f, _ in capi.KpstmLaunch._fields_ if f != "reserved"}
 
-    def set_launch(self, tile_px: int = 0, samples_per_lane: int = 0, persistent: int = 0, graph: int = 0) -> None:
+    def set_launch(self, tile_px: int = 0, samples_per_lane: int = 0, persistent: int = 0, graph: int = 0,
+                   ctas_per_sm: int = 0) -> None:
         """Imaging work split (kpstm_set_launch); results are identical for every choice."""
         cfg = capi.KpstmLaunch(tile_px=tile_px, samples_per_lane=samples_per_lane, persistent=persistent,
-                               graph=graph)
+                               graph=graph, ctas_per_sm=ctas_per_sm)
         capi.check("kpstm_set_launch", self._lib.kpstm_set_launch(self._h, C.byref(cfg)))
 
     def autotune(self, d_hdr_be: int, d_samples: int, ntr: int) -> tuple[dict, float]:

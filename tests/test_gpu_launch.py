@@ -64,11 +64,14 @@ def test_launch_configs_bit_identical(kpstm_lib, mode, prec):
     prm = dict(precision=prec)
     ref = _image(s, prm)
     assert ref["pairs"] > 0
-    for px, K, pers in itertools.product((1, 2, 4, 8), _valid_K(mode, prec), (0, 1)):
-        g = _image(s, prm, dict(tile_px=px, samples_per_lane=K, persistent=pers))
+    for px, K, pers, ctas in itertools.product((1, 2, 4, 8), _valid_K(mode, prec), (0, 1), (2, 3)):
+        if ctas == 3 and not (mode == capi.MODE_FULL and prec == capi.PREC_FP32 and K <= 16):
+            continue
+        g = _image(s, prm, dict(tile_px=px, samples_per_lane=K, persistent=pers, ctas_per_sm=ctas))
         assert g["cfg"]["tile_px"] == px and g["cfg"]["samples_per_lane"] == K
-        assert np.array_equal(g["km"], ref["km"]), (px, K, pers)
-        assert np.array_equal(g["fold"], ref["fold"]), (px, K, pers)
+        assert g["cfg"]["ctas_per_sm"] == ctas
+        assert np.array_equal(g["km"], ref["km"]), (px, K, pers, ctas)
+        assert np.array_equal(g["fold"], ref["fold"]), (px, K, pers, ctas)
         assert g["pairs"] == ref["pairs"]
 
 
@@ -88,7 +91,7 @@ def test_set_launch_rejects_bad_values(kpstm_lib):
     s = _survey(capi.MODE_FULL, ntr=10)
     with Migration(s.params, s.velocity) as m:
         for bad in (dict(tile_px=3), dict(samples_per_lane=32), dict(samples_per_lane=12), dict(persistent=2),
-                    dict(graph=-1)):
+                    dict(graph=-1), dict(ctas_per_sm=4), dict(ctas_per_sm=3, samples_per_lane=24)):
             with pytest.raises(capi.KpstmError) as e:
                 m.set_launch(**bad)
             assert e.value.status == 1  # KPSTM_ERR_INVALID_ARG
