@@ -210,9 +210,11 @@ int kpstm_profile_read(kpstm_ctx *ctx, kpstm_profile *out);
    order, so all configurations give bit-identical images. */
 typedef struct {
     int tile_px;          /* patch columns along the inline axis: 1, 2, 4 or 8
-                             (tile_py = 8 / tile_px); 0 = default */
+                             (tile_py = 8 / tile_px); 0 = default (the fewest
+                             tiles, ties to 4 x 2) */
     int samples_per_lane; /* 8, 16, 24 or 32 (full mode <= 24, BF16/Kahan <= 16);
-                             0 = default (the fewest windows, then the smallest K) */
+                             0 = default (the fewest windows, then the smallest K,
+                             at most 16 with 3 CTAs per SM) */
     int persistent;       /* 1: one resident grid takes (class, tile, window) items
                              from a device counter, largest classes first;
                              0: one CTA per item */
@@ -220,10 +222,11 @@ typedef struct {
                              tap tables, imaging) is captured once per block shape
                              into a CUDA graph and replayed; ignored while
                              profiling is enabled */
-    int ctas_per_sm;      /* imaging kernel variant: 2 (default; 0 = 2) or 3 resident
-                             CTAs per SM - 3 trades register space (80 per thread, so
+    int ctas_per_sm;      /* imaging kernel variant: 2 or 3 resident CTAs per SM -
+                             3 trades register space (80 per thread, so
                              samples_per_lane <= 16) and pipeline depth for 24
-                             resident warps; full mode with fp32 storage only */
+                             resident warps; full mode with fp32 storage only;
+                             0 = default (3 where allowed, else 2) */
     int reserved[3];
 } kpstm_launch;
 int kpstm_get_launch(const kpstm_ctx *ctx, kpstm_launch *cfg);

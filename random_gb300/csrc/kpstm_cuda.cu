@@ -263,14 +263,15 @@ static int default_K(const kpstm_params *p)
     return per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
 }
 
-/* default patch: the fewest tiles (fewest idle warps), ties to the
-   consecutive-crossline patch 1 x 8 */
+/* default patch: the fewest tiles (fewest idle warps), ties to the 4 x 2
+   patch, then 2 x 4, 8 x 1, 1 x 8 (4 x 2 measured fastest on the 3-D survey) */
 static int default_px(const kpstm_setup *s)
 {
-    int best = 1;
+    static const int order[4] = {4, 2, 8, 1};
+    int best = 4;
     int64_t bn = -1;
-    for (int px = 1; px <= 8; px *= 2) {
-        const int py = 8 / px;
+    for (int o = 0; o < 4; ++o) {
+        const int px = order[o], py = 8 / px;
         const int64_t n = (int64_t)((s->dims.nx + px - 1) / px) * ((s->dims.ny + py - 1) / py);
         if (bn < 0 || n < bn) {
             bn = n;
@@ -555,8 +556,10 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     cudaGetDevice(&c->device);
     const int ns = params->ns, tm = s.dims.trange_max;
     const int ncol = s.ncol;
-    set_K(c, default_K(params));
-    c->minb = 2;
+    /* full mode with fp32 storage: the 3-CTAs-per-SM variant (K <= 16), measured
+       faster than 2 CTAs with K = 24 on the 3-D survey */
+    c->minb = (params->mode == KPSTM_MODE_FULL && params->precision == KPSTM_PREC_FP32) ? 3 : 2;
+    set_K(c, c->minb == 3 && default_K(params) > 16 ? 16 : default_K(params));
     {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -1046,15 +1049,15 @@ extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
 {
     if (!c || !cfg) return KPSTM_ERR_INVALID_ARG;
     const int px = cfg->tile_px ? cfg->tile_px : default_px(&c->s);
-    const int minb = cfg->ctas_per_sm ? cfg->ctas_per_sm : 2;
+    const bool occ3 = c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32;
+    const int minb = cfg->ctas_per_sm ? cfg->ctas_per_sm : (occ3 ? 3 : 2);
     int K = cfg->samples_per_lane ? cfg->samples_per_lane : default_K(&c->p);
     if (minb == 3 && !cfg->samples_per_lane && K > 16) K = 16;
     if ((px != 1 && px != 2 && px != 4 && px != 8) || !valid_K(c, K)) return KPSTM_ERR_INVALID_ARG;
     if ((cfg->persistent != 0 && cfg->persistent != 1) || (cfg->graph != 0 && cfg->graph != 1))
         return KPSTM_ERR_INVALID_ARG;
     if (minb != 2 && minb != 3) return KPSTM_ERR_INVALID_ARG;
-    if (minb == 3 && !(c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32 && K <= 16))
-        return KPSTM_ERR_INVALID_ARG;
+    if (minb == 3 && !(occ3 && K <= 16)) return KPSTM_ERR_INVALID_ARG;
     drop_graphs(c);
     if (px != c->tile_px) {
         int st = set_tiles(c, px);
@@ -1318,7 +1321,12 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
         a.kc = c->d_lkc;
         a.cnt = c->d_lcnt;
         a.hits = c->d_lhits;
+        /* the adjoint's own split: 2 CTAs/SM and the largest K of the hi/lo
+           tables (the imaging launch may use the 3-CTA variant's K <= 16) */
+        const int K0 = c->K;
+        set_K(c, default_K(&c->p));
         cudaError_t e = launch_image(c, a, ncls, true);
+        set_K(c, K0);
         KP_CUDA(e);
     }
     k_relayout<<<1024, 256, 0, c->cs>>>(c->d_lkm, nullptr, c->d_tscale, ncol, ncls, ns, d_model);
