@@ -251,13 +251,13 @@ def run_ours(args, rank, world, local_rank):
     achieved = b_alg / t_launch / 1e9
     pairs_per_launch = pairs / launches
     # DRAM traffic per launch from ncu (dram__bytes_read + write) of a
-    # 5,000-trace launch of this kernel into the same image: 4.080e9 bytes, of
-    # which the tap tables are 5,000 rows; the accumulator part is fixed, the
-    # table part grows with the traces of the launch
-    traffic = 4.080e9 + (block - 5000) * row_floats * 4
+    # 5,000-trace launch of the default kernel (3 CTAs/SM, K = 16) into the same
+    # image: 4.194e9 bytes, of which the tap tables are 5,000 rows; the
+    # accumulator part is fixed, the table part grows with the traces
+    traffic = 4.194e9 + (block - 5000) * row_floats * 4
     # issue-slot roofline: warp instructions per pair from the same capture
-    # (55.2 per 32 pairs) against 4 schedulers x SMs x the SM clock
-    instr_per_pair = 55.2 / 32
+    # (56.1 per 32 pairs) against 4 schedulers x SMs x the SM clock
+    instr_per_pair = 56.1 / 32
     issue_peak = 4 * 152 * (clk.get("sm_mhz") or peaks["sm_max_mhz"]) * 1e6
     issue_achieved = pairs_per_launch / t_launch * instr_per_pair
     roofline = {
