@@ -4,7 +4,6 @@ reference checkout is present - fresh runs of the compiled reference on
 random small configurations."""
 from __future__ import annotations
 
-import os
 import tempfile
 from pathlib import Path
 
@@ -60,7 +59,9 @@ def test_prep_trace_mirror_and_tail(oracle_lib):
     assert P[tm] == f[0]
 
 
-ref_present = Path(os.environ.get("KPSTM_REFERENCE_DIR", "/root/reference"), "Kirchhoff.c").exists()
+from oracle.refbuild import REFERENCE_SOURCE  # noqa: E402  (the recipe owns the reference location)
+
+ref_present = REFERENCE_SOURCE.exists()
 
 
 @pytest.mark.skipif(not ref_present, reason="reference checkout absent")
