@@ -324,6 +324,14 @@ int kpstm_segy_info(const void *file_bytes, int64_t nbytes, int32_t *ns, float *
    xc, yc, class order.  dst must hold dims.nx*dims.ny*nh*(240+4*ns) bytes. */
 int kpstm_write_su(const kpstm_ctx *ctx, const float *image, void *dst, int64_t dst_bytes);
 
+/* Front headers of the output SEG-Y file, write_segy_ebdic_header
+   (Kirchhoff.c:729-814): 3200 text bytes and the 400-byte binary header
+   (sample interval, samples per trace, format 5 = IEEE float).  The
+   reference's combine script (Kirchhoff.c:821-874) writes them followed by
+   the slabs' SU records (kpstm_write_su) in job order.  dst must hold 3600
+   bytes.  Needs no device. */
+int kpstm_segy_front_headers(const kpstm_params *params, void *dst, int64_t dst_bytes);
+
 const char *kpstm_strerror(int status);
 int kpstm_abi_version(void);
 

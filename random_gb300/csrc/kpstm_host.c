@@ -278,3 +278,41 @@ int kpstm_su_headers(const kpstm_params *p, const kpstm_setup *s, int32_t col, i
     put_be32(h + 236, 9999);
     return KPSTM_OK;
 }
+
+/* Front headers of the output SEG-Y file, write_segy_ebdic_header
+   (Kirchhoff.c:729-814): a 3200-byte text header and a 400-byte binary header
+   that the combine script (:821-874) places before the slabs' SU records.
+   Text: the reference formats two lines into the same buffer, so the second
+   overwrites the start of the first ("written by G. O'Brien\n", NUL, then
+   the tail "from prototype code\n" and its NUL: bytes 0-43); it leaves the
+   rest of the 3200 bytes uninitialised, written as zeros here.  Binary header (16-bit
+   big-endian words): 3213 traces per ensemble (the reference computes
+   Nx*Ny*nh but writes an uninitialised short; the value is written here,
+   truncated to 16 bits), 3217 sample interval in us, 3221 and 3223 samples
+   per trace, 3225 format 5 (IEEE float), 3227, 3229, 3231 = 1; the rest
+   zero. */
+int kpstm_segy_front_headers(const kpstm_params *p, void *dst, int64_t dst_bytes)
+{
+    if (!p || !dst) return KPSTM_ERR_INVALID_ARG;
+    if (dst_bytes < 3600) return KPSTM_ERR_INVALID_ARG;
+    kpstm_setup s;
+    int st = kpstm_setup_of(p, &s);
+    if (st) return st;
+    uint8_t *o = (uint8_t *)dst;
+    memset(o, 0, 3600);
+    static const char first[] = "outputting cdp gathers from prototype code\n";
+    static const char second[] = "written by G. O'Brien\n";
+    memcpy(o, first, sizeof(first));   /* with its NUL */
+    memcpy(o, second, sizeof(second)); /* over the start, with its NUL */
+    uint8_t *b = o + 3200;
+    const int64_t ntr = (int64_t)s.dims.Nx * s.dims.Ny * s.dims.nh;
+    put_be16(b + 12, (uint16_t)ntr);
+    put_be16(b + 16, (uint16_t)(p->dt * 1000000));
+    put_be16(b + 20, (uint16_t)p->ns);
+    put_be16(b + 22, (uint16_t)p->ns);
+    put_be16(b + 24, 5);
+    put_be16(b + 26, 1);
+    put_be16(b + 28, 1);
+    put_be16(b + 30, 1);
+    return KPSTM_OK;
+}

@@ -186,3 +186,27 @@ def migrate(survey, params: dict | None = None, block: int = 50000, want_acc: bo
         if want_acc:
             out["km"], out["fold_acc"] = m.accumulators()
         return out
+
+
+def segy_front_headers(params: dict) -> bytes:
+    """The 3600 front-header bytes of the output SEG-Y file
+    (kpstm_segy_front_headers; no device needed)."""
+    lib = capi.load()
+    prm = capi.make_params(params)
+    buf = np.zeros(3600, np.uint8)
+    capi.check("kpstm_segy_front_headers", lib.kpstm_segy_front_headers(C.byref(prm), buf.ctypes.data, buf.size))
+    return buf.tobytes()
+
+
+def combine_su(out_path, params: dict, slab_files) -> None:
+    """The reference's combine step (Kirchhoff.c:821-874): front headers,
+    then each slab's SU records (image<job>.su) in job order, into one file."""
+    with open(out_path, "wb") as out:
+        out.write(segy_front_headers(params))
+        for f in slab_files:
+            with open(f, "rb") as src:
+                while True:
+                    chunk = src.read(1 << 24)
+                    if not chunk:
+                        break
+                    out.write(chunk)
