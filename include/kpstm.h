@@ -319,6 +319,16 @@ int kpstm_ibm_to_ieee(const uint32_t *ibm_be, float *out, int64_t n);
 int kpstm_segy_info(const void *file_bytes, int64_t nbytes, int32_t *ns, float *dt,
                     int64_t *ntraces);
 
+/* The gridded v_rms model from a velocity SEG-Y file image in memory,
+   build_vel_model (Kirchhoff.c:447-626): header words 47/48 (iline, xline)
+   pick the cell (truncating division, as :539), samples IBM-decoded; a later
+   trace overwrites an earlier one, unreached cells are 0.  vrms receives
+   [n_iline][n_xline][nsm] floats (nsm from kpstm_segy_info), ready for
+   kpstm_velocity.vrms.  Needs no device. */
+int kpstm_velocity_from_segy(const void *file_bytes, int64_t nbytes, int32_t n_iline, int32_t n_xline,
+                             int32_t o_iline, int32_t o_xline, int32_t d_iline, int32_t d_xline, float *vrms,
+                             int64_t vrms_elems);
+
 /* SU trace records of a finished image, Kirchhoff.c:1482-1593: 240-byte
    big-endian header plus ns big-endian floats per output trace, traces in
    xc, yc, class order.  dst must hold dims.nx*dims.ny*nh*(240+4*ns) bytes. */

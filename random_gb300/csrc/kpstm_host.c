@@ -316,3 +316,39 @@ int kpstm_segy_front_headers(const kpstm_params *p, void *dst, int64_t dst_bytes
     put_be16(b + 30, 1);
     return KPSTM_OK;
 }
+
+/* build_vel_model (Kirchhoff.c:447-626): the gridded v_rms model from the
+   velocity SEG-Y file image.  Sampling from the first trace header (:482-489,
+   as kpstm_segy_info); for every trace in file order, header words 47 and 48
+   (iline, xline, :537-538) give the cell (iline - o_iline) / d_iline,
+   (xline - o_xline) / d_xline with C's truncating division (:539), and a cell
+   inside the grid takes the trace's IBM-decoded samples (:524-530, 544) - a
+   later trace overwrites an earlier one; cells no trace reaches stay 0 (the
+   reference's calloc), which kpstm_create then reports as a zero velocity
+   where a column needs it.  vrms: [n_iline][n_xline][nsm] floats, nsm from
+   kpstm_segy_info. */
+int kpstm_velocity_from_segy(const void *file_bytes, int64_t nbytes, int32_t n_iline, int32_t n_xline,
+                             int32_t o_iline, int32_t o_xline, int32_t d_iline, int32_t d_xline, float *vrms,
+                             int64_t vrms_elems)
+{
+    int32_t nsm = 0;
+    float dtm = 0.0f;
+    int64_t ntm = 0;
+    int st = kpstm_segy_info(file_bytes, nbytes, &nsm, &dtm, &ntm);
+    if (st) return st;
+    if (!vrms || n_iline <= 0 || n_xline <= 0 || d_iline == 0 || d_xline == 0) return KPSTM_ERR_INVALID_ARG;
+    if (vrms_elems < (int64_t)n_iline * n_xline * nsm) return KPSTM_ERR_INVALID_ARG;
+    memset(vrms, 0, sizeof(float) * (size_t)n_iline * n_xline * nsm);
+    const uint8_t *b = (const uint8_t *)file_bytes + 3600;
+    const int64_t rec = 240 + 4 * (int64_t)nsm;
+    for (int64_t k = 0; k < ntm; ++k) {
+        const uint8_t *r = b + k * rec;
+        const int32_t iline = (int32_t)(((uint32_t)r[188] << 24) | ((uint32_t)r[189] << 16) | ((uint32_t)r[190] << 8) | r[191]);
+        const int32_t xline = (int32_t)(((uint32_t)r[192] << 24) | ((uint32_t)r[193] << 16) | ((uint32_t)r[194] << 8) | r[195]);
+        const int32_t i = (iline - o_iline) / d_iline, j = (xline - o_xline) / d_xline;
+        if (i < 0 || i >= n_iline || j < 0 || j >= n_xline) continue;
+        st = kpstm_ibm_to_ieee((const uint32_t *)(const void *)(r + 240), vrms + ((int64_t)i * n_xline + j) * nsm, nsm);
+        if (st) return st;
+    }
+    return KPSTM_OK;
+}

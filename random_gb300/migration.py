@@ -210,3 +210,19 @@ def combine_su(out_path, params: dict, slab_files) -> None:
                     if not chunk:
                         break
                     out.write(chunk)
+
+
+def velocity_from_segy(file_bytes: bytes, n_iline: int, n_xline: int, o_iline: int, o_xline: int, d_iline: int,
+                       d_xline: int):
+    """build_vel_model from a velocity SEG-Y file image: returns (vrms
+    [n_iline, n_xline, nsm] float32, nsm, dtm) via kpstm_velocity_from_segy."""
+    lib = capi.load()
+    raw = np.frombuffer(file_bytes, np.uint8)
+    ns, dt, ntr = C.c_int32(), C.c_float(), C.c_int64()
+    capi.check("kpstm_segy_info", lib.kpstm_segy_info(raw.ctypes.data, raw.size, C.byref(ns), C.byref(dt),
+                                                      C.byref(ntr)))
+    out = np.zeros((n_iline, n_xline, ns.value), np.float32)
+    capi.check("kpstm_velocity_from_segy",
+               lib.kpstm_velocity_from_segy(raw.ctypes.data, raw.size, n_iline, n_xline, o_iline, o_xline, d_iline,
+                                            d_xline, out.ctypes.data, out.size))
+    return out, ns.value, dt.value

@@ -56,3 +56,24 @@ def test_front_headers_and_combine_match_the_reference(kpstm_lib):
         script = (img / "combine_script").read_text().split("\n")
         assert script[0].startswith("cat ebdic_header.bin binary_header.bin")
         assert [ln.split()[1] for ln in script[1:1 + jobs]] == [f"image{j}.su" for j in range(jobs)]
+
+
+def test_velocity_loader_reads_the_written_model(kpstm_lib, tmp_path):
+    """The velocity file the harness writes for the reference, read back
+    with build_vel_model's binning, equals the grid it was written from."""
+    from random_gb300.migration import velocity_from_segy
+    s = synth.patch3d(ntr=20, ns=151, dt=0.004, nx=6, ny=4, bin_m=25.0, max_offset=600.0, n_refl=1, n_diff=1,
+                      aperture=200.0, seed=4)
+    s.write_files(tmp_path / "d.segy", tmp_path / "v.segy")
+    v = s.velocity
+    got, nsm, dtm = velocity_from_segy((tmp_path / "v.segy").read_bytes(), v.n_iline, v.n_xline, v.o_iline,
+                                       v.o_xline, v.d_iline, v.d_xline)
+    assert nsm == v.nsm and dtm == np.float32(v.dtm)
+    assert np.array_equal(got.view(np.uint32), np.asarray(v.vrms, np.float32).reshape(got.shape).view(np.uint32))
+    # a grid larger than the file: the extra cells stay 0; a shifted origin drops rows
+    got2, _, _ = velocity_from_segy((tmp_path / "v.segy").read_bytes(), v.n_iline + 2, v.n_xline, v.o_iline,
+                                    v.o_xline, v.d_iline, v.d_xline)
+    assert np.array_equal(got2[:v.n_iline], got) and not got2[v.n_iline:].any()
+    got3, _, _ = velocity_from_segy((tmp_path / "v.segy").read_bytes(), v.n_iline, v.n_xline, v.o_iline + 2,
+                                    v.o_xline, v.d_iline, v.d_xline)
+    assert np.array_equal(got3[:v.n_iline - 2], got[2:]) and not got3[v.n_iline - 2:].any()
