@@ -110,7 +110,12 @@ typedef struct {
     int32_t output;     /* kpstm_output */
     /* KPSTM_MODE_FULL only: largest triangle half-width in samples (0 = trangeMax) */
     int32_t aa_max_halfwidth;
-    int32_t reserved[7];
+    /* KPSTM_MODE_FULL only: 0 = the reference's nearest grid node and nearest
+       velocity sample (Kirchhoff.c:1357-1378); 1 = trilinear interpolation of
+       v_rms at the same continuous grid position and time that the reference
+       rounds (clamped to the grid; below-grid columns are still refused) */
+    int32_t velocity_interp;
+    int32_t reserved[6];
 } kpstm_params;
 
 /* Gridded v_rms model, build_vel_model (Kirchhoff.c:22-27, 447-626).  Values

@@ -29,6 +29,8 @@ int ko_dims_of(const kpstm_params *p, ko_dims *d)
 {
     if (!p || !d || p->ns <= 0 || !(p->dt > 0) || p->jobs_x <= 0 || p->jobs_y <= 0 || p->nh <= 0)
         return KPSTM_ERR_INVALID_ARG;
+    if (p->velocity_interp != 0 && p->velocity_interp != 1) return KPSTM_ERR_INVALID_ARG;
+    if (p->velocity_interp && p->mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED;
     memset(d, 0, sizeof(*d));
     int Nx = p->inc_iline == 0 ? 1 : (int)ceil((p->end_iline - p->start_iline) / p->inc_iline);
     int Ny = p->inc_xline == 0 ? 1 : (int)ceil((p->end_xline - p->start_xline) / p->inc_xline);
@@ -97,6 +99,54 @@ typedef struct {
     int off, live;
 } ko_geom;
 
+/* v_rms of image column (xg, yg) (global column indices) at every output
+   sample t, in double.  Nearest (velocity_interp = 0): the grid node and the
+   velocity sample the reference rounds to (Kirchhoff.c:1357-1378).
+   Trilinear (velocity_interp = 1, full mode): the same continuous grid
+   position (integer division of the origin difference plus the column's
+   fractional step) and continuous sample t * (dt / dtm), clamped to the
+   grid.  Returns 0, or -1 where the rounded position is below the grid. */
+static int ko_col_vrms(const kpstm_params *p, const kpstm_velocity *v, int xg, int yg, int ns, double *out)
+{
+    const double gx = (p->start_iline - v->o_iline) / v->d_iline + xg * (p->inc_iline / v->d_iline);
+    const double gy = (p->start_xline - v->o_xline) / v->d_xline + yg * (p->inc_xline / v->d_xline);
+    int xc1 = (int)round(gx), yc1 = (int)round(gy);
+    if (xc1 > v->n_iline - 1) xc1 = v->n_iline - 1;
+    if (yc1 > v->n_xline - 1) yc1 = v->n_xline - 1;
+    if (xc1 < 0 || yc1 < 0) return -1;
+    const float step = p->dt / v->dtm;
+    if (!p->velocity_interp) {
+        const float *vr = v->vrms + ((size_t)xc1 * v->n_xline + yc1) * v->nsm;
+        for (int t = 0; t < ns; ++t) {
+            int q = (int)round((double)((float)t * step));
+            out[t] = vr[q > v->nsm - 1 ? v->nsm - 1 : q];
+        }
+        return 0;
+    }
+    const double cx = gx < 0 ? 0 : (gx > v->n_iline - 1 ? v->n_iline - 1 : gx);
+    const double cy = gy < 0 ? 0 : (gy > v->n_xline - 1 ? v->n_xline - 1 : gy);
+    const int i0 = (int)floor(cx), j0 = (int)floor(cy);
+    const int i1 = i0 + 1 < v->n_iline ? i0 + 1 : i0, j1 = j0 + 1 < v->n_xline ? j0 + 1 : j0;
+    const double wx = cx - i0, wy = cy - j0;
+    for (int t = 0; t < ns; ++t) {
+        double gt = (double)((float)t * step);
+        if (gt > v->nsm - 1) gt = v->nsm - 1;
+        const int k0 = (int)floor(gt), k1 = k0 + 1 < v->nsm ? k0 + 1 : k0;
+        const double wt = gt - k0;
+        double c[2];
+        for (int e = 0; e < 2; ++e) {
+            const int k = e ? k1 : k0;
+            const double a = v->vrms[((size_t)i0 * v->n_xline + j0) * v->nsm + k];
+            const double b = v->vrms[((size_t)i0 * v->n_xline + j1) * v->nsm + k];
+            const double cc = v->vrms[((size_t)i1 * v->n_xline + j0) * v->nsm + k];
+            const double dd = v->vrms[((size_t)i1 * v->n_xline + j1) * v->nsm + k];
+            c[e] = (1.0 - wx) * ((1.0 - wy) * a + wy * b) + wx * ((1.0 - wy) * cc + wy * dd);
+        }
+        out[t] = (1.0 - wt) * c[0] + wt * c[1];
+    }
+    return 0;
+}
+
 typedef struct {
     const kpstm_params *p;
     const kpstm_velocity *v;
@@ -144,7 +194,7 @@ static double full_tri(const float *f, int ns, double T, double Lf)
     return tri;
 }
 
-static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, const float *v2,
+static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, const float *vv_t,
                        const float *f, float *k, float *fo)
 {
     const kpstm_params *p = J->p;
@@ -155,7 +205,7 @@ static void full_pairs(const ko_job *J, const ko_geom *g, float IX, float IY, co
     const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
     const double ax = p->iline_distance / dt, ay = p->xline_distance / dt;
     for (int t = 0; t < ns; ++t) {
-        double rv2 = 1.0 / (double)v2[J->t1[t]];
+        double rv2 = 1.0 / (double)vv_t[t];
         double t0 = (double)t * dt;
         double th2 = 0.25 * t0 * t0;
         double as = th2 + dS2 * rv2, ar = th2 + dR2 * rv2;
@@ -182,6 +232,16 @@ static void *column_worker(void *arg)
     const ko_dims *d = J->d;
     const int ns = d->ns, nh = d->nh;
     int64_t pairs = 0;
+    double *vtmp = (double *)malloc(sizeof(double) * ns);
+    float *vvt = (float *)malloc(sizeof(float) * ns);
+    if (!vtmp || !vvt) {
+        free(vtmp);
+        free(vvt);
+        pthread_mutex_lock(&J->mu);
+        J->err = KPSTM_ERR_OUT_OF_MEMORY;
+        pthread_mutex_unlock(&J->mu);
+        return NULL;
+    }
     for (;;) {
         pthread_mutex_lock(&J->mu);
         int col = J->next_col++;
@@ -196,8 +256,15 @@ static void *column_worker(void *arg)
                              (yc + d->yslice * d->ny) * (p->inc_xline / J->v->d_xline));
         if (xc1 > J->v->n_iline - 1) xc1 = J->v->n_iline - 1;
         if (yc1 > J->v->n_xline - 1) yc1 = J->v->n_xline - 1;
-        const float *v2 = J->vel2 + ((size_t)xc1 * J->v->n_xline + yc1) * J->v->nsm;
+        const float *v2 = J->vel2 + ((size_t)(xc1 < 0 ? 0 : xc1) * J->v->n_xline + (yc1 < 0 ? 0 : yc1)) * J->v->nsm;
         int bad_vel = (xc1 < 0 || yc1 < 0);
+        if (p->mode == KPSTM_MODE_FULL && !bad_vel) {
+            /* v^2 per output sample as the product builds its rows: the nearest
+               node's float v^2, or the interpolated v_rms squared in double */
+            if (ko_col_vrms(p, J->v, xc + d->xslice * d->nx, yc + d->yslice * d->ny, ns, vtmp)) bad_vel = 1;
+            for (int t = 0; t < ns && !bad_vel; ++t)
+                vvt[t] = p->velocity_interp ? (float)(vtmp[t] * vtmp[t]) : v2[J->t1[t]];
+        }
         float *km = J->km + (size_t)col * nh * ns;
         float *fold = J->fold + (size_t)col * nh * ns;
         for (int64_t it = 0; it < J->ntr; ++it) {
@@ -216,7 +283,7 @@ static void *column_worker(void *arg)
             float *k = km + (size_t)g->off * ns;
             float *f = fold + (size_t)g->off * ns;
             if (p->mode == KPSTM_MODE_FULL) {
-                full_pairs(J, g, IX, IY, v2, J->P + (size_t)it * ns, k, f);
+                full_pairs(J, g, IX, IY, vvt, J->P + (size_t)it * ns, k, f);
                 pairs += ns;
                 continue;
             }
@@ -235,6 +302,8 @@ static void *column_worker(void *arg)
             pairs += ns;
         }
     }
+    free(vtmp);
+    free(vvt);
     pthread_mutex_lock(&J->mu);
     J->pairs += pairs;
     pthread_mutex_unlock(&J->mu);
@@ -422,7 +491,12 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
     if (direction == 0) memset(out, 0, sizeof(double) * nmod);
     else memset(out, 0, sizeof(double) * (size_t)ntr * ns);
     int *t1 = (int *)malloc(sizeof(int) * ns);
-    if (!t1) return KPSTM_ERR_OUT_OF_MEMORY;
+    double *vcol = (double *)malloc(sizeof(double) * ns);
+    if (!t1 || !vcol) {
+        free(t1);
+        free(vcol);
+        return KPSTM_ERR_OUT_OF_MEMORY;
+    }
     for (int t = 0; t < ns; ++t) {
         int q = (int)round((double)((float)t * (p->dt / v->dtm)));
         t1[t] = q > v->nsm - 1 ? v->nsm - 1 : q;
@@ -460,22 +534,21 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
                 float cdx = IX - g.cmpx, cdy = IY - g.cmpy;
                 float dC = sqrtf(cdx * cdx + cdy * cdy);
                 if (!((double)dC < p->aperture)) continue;
-                int xc1 = (int)round((p->start_iline - v->o_iline) / v->d_iline +
-                                     (xc + d.xslice * d.nx) * (p->inc_iline / v->d_iline));
-                int yc1 = (int)round((p->start_xline - v->o_xline) / v->d_xline +
-                                     (yc + d.yslice * d.ny) * (p->inc_xline / v->d_xline));
-                if (xc1 > v->n_iline - 1) xc1 = v->n_iline - 1;
-                if (yc1 > v->n_xline - 1) yc1 = v->n_xline - 1;
-                if (xc1 < 0 || yc1 < 0) { st = KPSTM_ERR_VELOCITY_RANGE; break; }
-                const float *vr = v->vrms + ((size_t)xc1 * v->n_xline + yc1) * v->nsm;
+                if (ko_col_vrms(p, v, xc + d.xslice * d.nx, yc + d.yslice * d.ny, ns, vcol)) {
+                    st = KPSTM_ERR_VELOCITY_RANGE;
+                    break;
+                }
                 const double sx = (double)IX - g.sxt, sy = (double)IY - g.syt;
                 const double gx = (double)IX - g.gxt, gy = (double)IY - g.gyt;
                 const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
                 const size_t mbase = (((size_t)xc * d.ny + yc) * nh + off) * ns;
                 const size_t dbase = (size_t)it * ns;
                 for (int t = 1; t < ns; ++t) {
-                    float vf = vr[t1[t]];
-                    double rv2 = 1.0 / (double)(vf * vf);
+                    /* v^2 as the product stores it: the node's float square, or
+                       the interpolated v_rms squared in double, rounded to float */
+                    const float vvf = p->velocity_interp ? (float)(vcol[t] * vcol[t])
+                                                         : (float)vcol[t] * (float)vcol[t];
+                    double rv2 = 1.0 / (double)vvf;
                     double t0 = (double)t * dt;
                     double th2 = 0.25 * t0 * t0;
                     double ts = sqrt(th2 + dS2 * rv2), tr = sqrt(th2 + dR2 * rv2);
@@ -508,6 +581,7 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
         }
     }
     free(t1);
+    free(vcol);
     return st;
 }
 
@@ -542,6 +616,13 @@ static void *column_worker64(void *arg)
     const ko_dims *d = J->d;
     const int ns = d->ns, nh = d->nh;
     const double dt = (double)p->dt;
+    double *vcol = (double *)malloc(sizeof(double) * ns);
+    if (!vcol) {
+        pthread_mutex_lock(&J->mu);
+        J->err = KPSTM_ERR_OUT_OF_MEMORY;
+        pthread_mutex_unlock(&J->mu);
+        return NULL;
+    }
     for (;;) {
         pthread_mutex_lock(&J->mu);
         int col = J->next_col++;
@@ -550,12 +631,8 @@ static void *column_worker64(void *arg)
         const int xc = col / d->ny, yc = col % d->ny;
         const double IX = (p->start_iline + ((xc + d->xslice * d->nx) * p->inc_iline)) * p->iline_distance;
         const double IY = (p->start_xline + ((yc + d->yslice * d->ny) * p->inc_xline)) * p->xline_distance;
-        int xc1 = (int)round((p->start_iline - v->o_iline) / v->d_iline + (xc + d->xslice * d->nx) * (p->inc_iline / v->d_iline));
-        int yc1 = (int)round((p->start_xline - v->o_xline) / v->d_xline + (yc + d->yslice * d->ny) * (p->inc_xline / v->d_xline));
-        if (xc1 > v->n_iline - 1) xc1 = v->n_iline - 1;
-        if (yc1 > v->n_xline - 1) yc1 = v->n_xline - 1;
-        const int bad = xc1 < 0 || yc1 < 0;
-        const float *vr = bad ? NULL : v->vrms + ((size_t)xc1 * v->n_xline + yc1) * v->nsm;
+        /* v_rms per output sample (nearest node and sample, or trilinear) */
+        const int bad = ko_col_vrms(p, v, xc + d->xslice * d->nx, yc + d->yslice * d->ny, ns, vcol) != 0;
         for (int64_t it = 0; it < J->ntr; ++it) {
             const ko_geom64 *g = &J->geom[it];
             if (!g->live) continue;
@@ -573,7 +650,7 @@ static void *column_worker64(void *arg)
             const double *D = J->D ? J->D + (size_t)it * ns : NULL;
             const float *f = J->samples + (size_t)it * ns;
             for (int t = 0; t < ns; ++t) {
-                const double vv = (double)vr[J->t1[t]] * (double)vr[J->t1[t]];
+                const double vv = vcol[t] * vcol[t];
                 if (!J->full) {
                     const double dsr = sqrt(J->t2[t] + dS2 / vv) + sqrt(J->t2[t] + dR2 / vv);
                     const double Tq = floor(dsr / dt);
@@ -598,6 +675,7 @@ static void *column_worker64(void *arg)
             }
         }
     }
+    free(vcol);
     return NULL;
 }
 

@@ -43,7 +43,7 @@ class KpstmParams(C.Structure):
         ("aperture", C.c_double), ("anti_alias_cutoff", C.c_double),
         ("jobs_x", C.c_int32), ("jobs_y", C.c_int32), ("job_id", C.c_int32),
         ("mode", C.c_int32), ("precision", C.c_int32), ("output", C.c_int32),
-        ("aa_max_halfwidth", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("aa_max_halfwidth", C.c_int32), ("velocity_interp", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 

@@ -607,6 +607,21 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
         st = kpstm_lowpass_kernel(params, hd);
         if (st) break;
         for (int t = 0; t < ns; ++t) hf[t] = (float)hd[t];
+        if (params->velocity_interp) {
+            /* one interpolated row per column */
+            vrows = (float2 *)malloc(sizeof(float2) * (size_t)ncol * ns);
+            if (!vrows) {
+                st = KPSTM_ERR_OUT_OF_MEMORY;
+                break;
+            }
+            st = kpstm_interp_rows(params, vel, &s, colrow, reinterpret_cast<float *>(vrows));
+            if (st) break;
+            for (int cc = 0; cc < ncol; ++cc)
+                if (colrow[cc] >= 0) colrow[cc] = cc;
+            nrow = ncol;
+            for (int L = 0; L < 64; ++L) invl2[L] = L > 0 ? 1.0f / (float)(L * L) : 0.0f;
+            break;
+        }
         /* compact the velocity rows the slab uses; v^2 in float as
            Kirchhoff.c:617, RN(1/v^2) for the exact division */
         int64_t ngrid = (int64_t)vel->n_iline * vel->n_xline;

@@ -119,6 +119,8 @@ int kpstm_segy_info(const void *file_bytes, int64_t nbytes, int32_t *ns, float *
 int kpstm_setup_of(const kpstm_params *p, kpstm_setup *s)
 {
     if (!p || !s) return KPSTM_ERR_INVALID_ARG;
+    if (p->velocity_interp != 0 && p->velocity_interp != 1) return KPSTM_ERR_INVALID_ARG;
+    if (p->velocity_interp && p->mode != KPSTM_MODE_FULL) return KPSTM_ERR_UNSUPPORTED; /* reference mode is exact */
     if (p->ns < 8 || p->ns > 32768 || !(p->dt > 0.0f) || p->nh <= 0 || p->nh > KPSTM_MAX_CLASSES ||
         p->jobs_x <= 0 || p->jobs_y <= 0 || p->job_id < 0 || p->job_id >= p->jobs_x * p->jobs_y ||
         !(p->iline_distance > 0) || !(p->xline_distance > 0) || !(p->dh != 0) ||
@@ -207,6 +209,64 @@ int kpstm_columns(const kpstm_params *p, const kpstm_velocity *v, const kpstm_se
             colrow[c] = (xc1 < 0 || yc1 < 0) ? -1 : xc1 * v->n_xline + yc1;
         }
     }
+    return KPSTM_OK;
+}
+
+/* Velocity rows of every column by trilinear interpolation of v_rms
+   (kpstm_params.velocity_interp = 1): at the continuous grid position the
+   reference rounds (Kirchhoff.c:1357-1365: integer division of the origin
+   difference plus the column's fractional step) and the continuous sample
+   t * (dt / dtm) it rounds (:1376-1378), each clamped to the grid; the
+   interpolated v_rms is squared in double and stored as float, with
+   RN(1/v^2) beside it.  rows: [ncol][ns] {v^2, 1/v^2}; columns whose rounded
+   position is below the grid keep colrow = -1 (refused when reached). */
+int kpstm_interp_rows(const kpstm_params *p, const kpstm_velocity *v, const kpstm_setup *s, const int32_t *colrow,
+                      float *rows2)
+{
+    const int nx = s->dims.nx, ny = s->dims.ny, ns = p->ns, nsm = v->nsm;
+    const float step = p->dt / v->dtm;
+    double *acc = (double *)malloc(sizeof(double) * (size_t)nsm);
+    if (!acc) return KPSTM_ERR_OUT_OF_MEMORY;
+    for (int xc = 0; xc < nx; ++xc)
+        for (int yc = 0; yc < ny; ++yc) {
+            const int c = xc * ny + yc;
+            float *row = rows2 + (size_t)c * 2 * ns;
+            if (colrow[c] < 0) {
+                for (int t = 0; t < ns; ++t) {
+                    row[2 * t] = 1.0f;
+                    row[2 * t + 1] = 1.0f;
+                }
+                continue;
+            }
+            double gx = (p->start_iline - v->o_iline) / v->d_iline + (xc + s->xslice * nx) * (p->inc_iline / v->d_iline);
+            double gy = (p->start_xline - v->o_xline) / v->d_xline + (yc + s->yslice * ny) * (p->inc_xline / v->d_xline);
+            gx = gx < 0.0 ? 0.0 : (gx > v->n_iline - 1 ? v->n_iline - 1 : gx);
+            gy = gy < 0.0 ? 0.0 : (gy > v->n_xline - 1 ? v->n_xline - 1 : gy);
+            const int i0 = (int)floor(gx), j0 = (int)floor(gy);
+            const int i1 = i0 + 1 < v->n_iline ? i0 + 1 : i0, j1 = j0 + 1 < v->n_xline ? j0 + 1 : j0;
+            const double wx = gx - i0, wy = gy - j0;
+            const float *v00 = v->vrms + ((size_t)i0 * v->n_xline + j0) * nsm;
+            const float *v01 = v->vrms + ((size_t)i0 * v->n_xline + j1) * nsm;
+            const float *v10 = v->vrms + ((size_t)i1 * v->n_xline + j0) * nsm;
+            const float *v11 = v->vrms + ((size_t)i1 * v->n_xline + j1) * nsm;
+            for (int k = 0; k < nsm; ++k)
+                acc[k] = (1.0 - wx) * ((1.0 - wy) * v00[k] + wy * v01[k]) + wx * ((1.0 - wy) * v10[k] + wy * v11[k]);
+            for (int t = 0; t < ns; ++t) {
+                double gt = (double)((float)t * step);
+                gt = gt > nsm - 1 ? nsm - 1 : gt;
+                const int k0 = (int)floor(gt), k1 = k0 + 1 < nsm ? k0 + 1 : k0;
+                const double wt = gt - k0;
+                const double vr = (1.0 - wt) * acc[k0] + wt * acc[k1];
+                const float vv = (float)(vr * vr);
+                if (!(vv > 0.0f)) {
+                    free(acc);
+                    return KPSTM_ERR_VELOCITY_ZERO;
+                }
+                row[2 * t] = vv;
+                row[2 * t + 1] = 1.0f / vv;
+            }
+        }
+    free(acc);
     return KPSTM_OK;
 }
 

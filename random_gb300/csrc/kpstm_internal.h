@@ -46,6 +46,8 @@ int kpstm_setup_of(const kpstm_params *p, kpstm_setup *s);
 int kpstm_velocity_check(const kpstm_params *p, const kpstm_velocity *v, const kpstm_setup *s);
 /* Column coordinates IX/IY (Kirchhoff.c:1346-1347) and velocity row of each
    column (Kirchhoff.c:1357-1365): colxy[2*ncol], colrow[ncol]. */
+int kpstm_interp_rows(const kpstm_params *p, const kpstm_velocity *v, const kpstm_setup *s, const int32_t *colrow,
+                      float *rows2);
 int kpstm_columns(const kpstm_params *p, const kpstm_velocity *v, const kpstm_setup *s,
                   float *colxy, int32_t *colrow);
 /* t2[t] (Kirchhoff.c:1247) and the velocity time index t1[t] (:1376-1378). */

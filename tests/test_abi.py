@@ -127,6 +127,11 @@ def test_create_rejects_bad_arguments_without_touching_a_gpu(kpstm_lib):
                               v0.ctypes.data)
     prm = capi.make_params(s.params)
     assert kpstm_lib.kpstm_create(C.byref(prm), C.byref(vel0), C.byref(h)) == 4
+    # velocity interpolation exists for the full operator only (reference mode is exact)
+    prm = capi.make_params(dict(s.params, velocity_interp=1))
+    assert kpstm_lib.kpstm_create(C.byref(prm), C.byref(vel), C.byref(h)) == 11  # KPSTM_ERR_UNSUPPORTED
+    prm = capi.make_params(dict(s.params, velocity_interp=2))
+    assert kpstm_lib.kpstm_create(C.byref(prm), C.byref(vel), C.byref(h)) == 1
     del keep
 
 

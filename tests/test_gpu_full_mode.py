@@ -65,3 +65,27 @@ def test_full_mode_block_split_is_invisible(kpstm_lib):
     a = migrate(s, block=100_000, want_acc=True)
     b = migrate(s, block=77, want_acc=True)
     assert np.array_equal(a["km"], b["km"]) and np.array_equal(a["fold"], b["fold"])
+
+
+def _coarse_velocity(s):
+    """The survey's v_rms grid kept on every second inline node and every
+    second time sample, so that columns fall between nodes."""
+    from random_gb300.synth import Velocity
+    v = s.velocity
+    vr = np.ascontiguousarray(v.vrms[::2, :, ::2])
+    return Velocity(n_iline=vr.shape[0], n_xline=v.n_xline, nsm=vr.shape[2], o_iline=v.o_iline,
+                    o_xline=v.o_xline, d_iline=2 * v.d_iline, d_xline=v.d_xline, dtm=2 * v.dtm, vrms=vr)
+
+
+def test_trilinear_velocity_matches_fp64_oracle(kpstm_lib, oracle_lib):
+    """velocity_interp = 1: v_rms interpolated (trilinear) at the position the
+    reference rounds; against the FP64 oracle with the same interpolation,
+    and visibly different from the nearest-node model."""
+    s = _survey(ntr=300, nx=9, ny=4, nh=1, dh=1e9, output=capi.OUT_STACK)
+    s.velocity = _coarse_velocity(s)
+    p = dict(velocity_interp=1)
+    g = migrate(s, p, want_acc=True)
+    o = oracle_lib.kirchhoff64(s, p)
+    assert rel_l2(g["km"], o["km"]) <= ACC_TOL, rel_l2(g["km"], o["km"])
+    near = migrate(s, want_acc=True)
+    assert rel_l2(near["km"], g["km"]) > 10 * ACC_TOL
