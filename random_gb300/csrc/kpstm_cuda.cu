@@ -40,7 +40,7 @@ struct kpstm_ctx {
     int device;
     int finished_state; /* reserved */
     cudaStream_t cs, xs;         /* compute, copy */
-    cudaEvent_t copy_done[2], comp_done[2];
+    cudaEvent_t copy_done[2], comp_done[2], decoded[2];
     int slot;
     int K, nwin;                 /* samples per lane, time windows */
     int64_t ntile;               /* image tiles of 8 columns */
@@ -81,7 +81,7 @@ struct kpstm_ctx {
     int64_t scap;
     int32_t *d_hdr[2];
     float *d_smp[2];
-    uint32_t *d_raw;
+    uint32_t *d_raw[2];          /* raw SEG-Y records, one per staging slot */
     int64_t rawcap;
     /* status */
     int *d_status;
@@ -662,6 +662,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
                 e = cudaEventCreateWithFlags(&c->copy_done[k], cudaEventDisableTiming);
                 if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->comp_done[k], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->decoded[k], cudaEventDisableTiming);
             }
             if (e != cudaSuccess) {
                 st = KPSTM_ERR_CUDA;
@@ -748,7 +749,7 @@ static int kp_free_all(kpstm_ctx *c)
     void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_tscale, c->d_c4, c->d_c4r,
                     c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
                     c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
-                    c->d_smp[1], c->d_raw, c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
+                    c->d_smp[1], c->d_raw[0], c->d_raw[1], c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
                     c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
                     c->d_lhits, c->d_dotpart, c->d_dot, c->d_smp16, c->d_scl16, c->d_tilecols, c->d_queue,
                     c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder, c->d_rvdt};
@@ -756,6 +757,7 @@ static int kp_free_all(kpstm_ctx *c)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
         if (c->copy_done[k]) cudaEventDestroy(c->copy_done[k]);
+        if (c->decoded[k]) cudaEventDestroy(c->decoded[k]);
         if (c->comp_done[k]) cudaEventDestroy(c->comp_done[k]);
     }
     drop_graphs(c);
@@ -850,20 +852,27 @@ extern "C" int kpstm_add_segy_block(kpstm_ctx *c, const void *rec, int64_t ntr)
     if (words > c->rawcap) {
         KP_CUDA(cudaStreamSynchronize(c->cs));
         KP_CUDA(cudaStreamSynchronize(c->xs));
-        cudaFree(c->d_raw);
-        c->d_raw = nullptr;
+        for (int k = 0; k < 2; ++k) {
+            cudaFree(c->d_raw[k]);
+            c->d_raw[k] = nullptr;
+        }
         c->rawcap = 0;
-        KP_CUDA(cudaMalloc(&c->d_raw, sizeof(uint32_t) * words));
-        c->rawcap = words;
+        const int64_t cap = words + words / 8;
+        KP_CUDA(cudaMalloc(&c->d_raw[0], sizeof(uint32_t) * cap));
+        KP_CUDA(cudaMalloc(&c->d_raw[1], sizeof(uint32_t) * cap));
+        c->rawcap = cap;
     }
     const int s = c->slot;
-    KP_CUDA(cudaStreamWaitEvent(c->xs, c->comp_done[s], 0));
-    KP_CUDA(cudaStreamWaitEvent(c->xs, c->comp_done[s ^ 1], 0)); /* single raw buffer */
-    KP_CUDA(cudaMemcpyAsync(c->d_raw, rec, sizeof(uint32_t) * words, cudaMemcpyHostToDevice, c->xs));
+    /* raw slot s is free once the block that last used it is decoded; the
+       header/sample slot s once that block is imaged, so the copy of this
+       block overlaps the imaging of the previous one */
+    KP_CUDA(cudaStreamWaitEvent(c->xs, c->decoded[s], 0));
+    KP_CUDA(cudaMemcpyAsync(c->d_raw[s], rec, sizeof(uint32_t) * words, cudaMemcpyHostToDevice, c->xs));
     KP_CUDA(cudaEventRecord(c->copy_done[s], c->xs));
     KP_CUDA(cudaStreamWaitEvent(c->cs, c->copy_done[s], 0));
-    k_segy_decode<<<1024, 256, 0, c->cs>>>(c->d_raw, ntr, c->p.ns, c->d_hdr[s], c->d_smp[s]);
+    k_segy_decode<<<1024, 256, 0, c->cs>>>(c->d_raw[s], ntr, c->p.ns, c->d_hdr[s], c->d_smp[s]);
     KP_CUDA(cudaGetLastError());
+    KP_CUDA(cudaEventRecord(c->decoded[s], c->cs));
     st = run_block(c, c->d_hdr[s], c->d_smp[s], ntr);
     if (st) return st;
     KP_CUDA(cudaEventRecord(c->comp_done[s], c->cs));

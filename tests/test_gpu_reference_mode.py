@@ -66,6 +66,14 @@ def test_segy_records_path(kpstm_lib):
         km, fold = m.accumulators()
     ref = migrate(s, want_acc=True)
     assert np.array_equal(km, ref["km"]) and np.array_equal(fold, ref["fold"])
+    # many blocks: both raw-record slots reused several times, blocks of
+    # different sizes (the copy of one block overlaps the previous imaging)
+    with Migration(s.params, s.velocity) as m:
+        edges = [0, 7, 30, 31, 60, 95, s.ntr]
+        for a, b in zip(edges[:-1], edges[1:]):
+            m.add_segy_block(rec[a:b])
+        km2, fold2 = m.accumulators()
+    assert np.array_equal(km2, ref["km"]) and np.array_equal(fold2, ref["fold"])
 
 
 def test_device_pointer_path(kpstm_lib):
