@@ -482,6 +482,21 @@ def run_lsm(args):
             "pairs_per_application": pairs_app,
             "config": {"traces": ntr, "ns": 751, "model": "200x200x751", "aperture_m": 3000.0},
             "clocks": clk}
+    if args.dot_test:
+        # adjointness at this size: |<L m, d> - <m, L^T d>| for seeded random m, d
+        gg = torch.Generator(device=dev)
+        gg.manual_seed(11)
+        mv = torch.randn(*m.shape, device=dev, generator=gg)
+        dv = torch.randn((ntr, 751), device=dev, generator=gg)
+        Lm = torch.empty_like(dv)
+        Ltd = torch.empty_like(mv)
+        m.lsm_forward(mv.data_ptr(), Lm.data_ptr())
+        m.lsm_adjoint(dv.data_ptr(), Ltd.data_ptr())
+        torch.cuda.synchronize()
+        a_ = float((Lm.double() * dv.double()).sum())
+        b_ = float((mv.double() * Ltd.double()).sum())
+        line["dot_test"] = {"rel": abs(a_ - b_) / abs(a_),
+                            "rel_to_norms": abs(a_ - b_) / float(Lm.double().norm() * dv.double().norm())}
     if args.cg_iters > 0:
         # least-squares migration of the survey's own events (bf16 data vectors,
         # FP64 CG scalars): time and residual history of --cg-iters iterations
@@ -542,6 +557,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cg-iters", type=int, default=0, help="lsm workload: also time this many CG iterations")
+    ap.add_argument("--dot-test", action="store_true", help="lsm workload: also run the dot-product test")
     ap.add_argument("--autotune", type=int, default=0,
                     help="survey workload: autotune the launch on this many traces before timing (0: default launch)")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
