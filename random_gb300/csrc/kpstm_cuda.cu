@@ -181,6 +181,10 @@ static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo, int minb)
         return nullptr;
     }
     if (kahan) {
+        if (full && minb == 3) {
+            if constexpr (K <= 8) return k_image<K, true, true, false, 3>;
+            return nullptr;
+        }
         if constexpr (K <= 16) return full ? k_image<K, true, true> : k_image<K, false, true>;
         return nullptr;
     }
@@ -253,6 +257,15 @@ static int kmax_of(const kpstm_params *p)
 {
     if (p->precision == KPSTM_PREC_BF16_KAHAN) return 16;
     return p->mode == KPSTM_MODE_FULL ? 24 : 32;
+}
+
+/* Largest samples-per-lane of the 3-CTAs-per-SM variant (80 registers, no
+   spills): full mode 16, full mode with Kahan sums 8; 0 where there is no
+   such variant. */
+static int occ3_kmax(const kpstm_params *p)
+{
+    if (p->mode != KPSTM_MODE_FULL) return 0;
+    return p->precision == KPSTM_PREC_BF16_KAHAN ? 8 : 16;
 }
 
 static int default_K(const kpstm_params *p)
@@ -1075,13 +1088,14 @@ extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
     const int px = cfg->tile_px ? cfg->tile_px : default_px(&c->s);
     const bool occ3 = c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32;
     const int minb = cfg->ctas_per_sm ? cfg->ctas_per_sm : (occ3 ? 3 : 2);
+    const int kmax3 = occ3_kmax(&c->p);
     int K = cfg->samples_per_lane ? cfg->samples_per_lane : default_K(&c->p);
-    if (minb == 3 && !cfg->samples_per_lane && K > 16) K = 16;
+    if (minb == 3 && !cfg->samples_per_lane && K > kmax3) K = kmax3;
     if ((px != 1 && px != 2 && px != 4 && px != 8) || !valid_K(c, K)) return KPSTM_ERR_INVALID_ARG;
     if ((cfg->persistent != 0 && cfg->persistent != 1) || (cfg->graph != 0 && cfg->graph != 1))
         return KPSTM_ERR_INVALID_ARG;
     if (minb != 2 && minb != 3) return KPSTM_ERR_INVALID_ARG;
-    if (minb == 3 && !(occ3 && K <= 16)) return KPSTM_ERR_INVALID_ARG;
+    if (minb == 3 && K > kmax3) return KPSTM_ERR_INVALID_ARG;
     drop_graphs(c);
     if (px != c->tile_px) {
         int st = set_tiles(c, px);
@@ -1123,8 +1137,7 @@ extern "C" int kpstm_autotune(kpstm_ctx *c, const int32_t *d_hdr_be, const float
             if (!valid_K(c, K)) continue;
             for (int v = 0; v < 4 && !st; ++v) {
                 const int pers = v & 1, minb = 2 + (v >> 1);
-                if (minb == 3 && !(c->p.mode == KPSTM_MODE_FULL && c->p.precision == KPSTM_PREC_FP32 && K <= 16))
-                    continue;
+                if (minb == 3 && K > occ3_kmax(&c->p)) continue;
                 kpstm_launch cfg;
                 memset(&cfg, 0, sizeof(cfg));
                 cfg.tile_px = px;
