@@ -229,9 +229,10 @@ typedef struct {
                              profiling is enabled */
     int ctas_per_sm;      /* imaging kernel variant: 2 or 3 resident CTAs per SM -
                              3 trades register space (80 per thread, so
-                             samples_per_lane <= 16, <= 8 with Kahan sums) and
-                             pipeline depth for 24 resident warps; full mode
-                             only; 0 = default (3 for fp32 storage, else 2) */
+                             samples_per_lane <= 16 in full mode, <= 8 with
+                             Kahan sums or in reference mode) and pipeline
+                             depth for 24 resident warps; 0 = default (3 for
+                             full mode with fp32 storage, else 2) */
     int reserved[3];
 } kpstm_launch;
 int kpstm_get_launch(const kpstm_ctx *ctx, kpstm_launch *cfg);

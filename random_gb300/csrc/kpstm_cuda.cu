@@ -180,6 +180,10 @@ static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo, int minb)
         }
         return nullptr;
     }
+    if (!full && minb == 3) {
+        if constexpr (K <= 8) return kahan ? k_image<K, false, true, false, 3> : k_image<K, false, false, false, 3>;
+        return nullptr;
+    }
     if (kahan) {
         if (full && minb == 3) {
             if constexpr (K <= 8) return k_image<K, true, true, false, 3>;
@@ -260,11 +264,10 @@ static int kmax_of(const kpstm_params *p)
 }
 
 /* Largest samples-per-lane of the 3-CTAs-per-SM variant (80 registers, no
-   spills): full mode 16, full mode with Kahan sums 8; 0 where there is no
-   such variant. */
+   spills): full mode 16, full mode with Kahan sums and the reference mode 8. */
 static int occ3_kmax(const kpstm_params *p)
 {
-    if (p->mode != KPSTM_MODE_FULL) return 0;
+    if (p->mode != KPSTM_MODE_FULL) return 8;
     return p->precision == KPSTM_PREC_BF16_KAHAN ? 8 : 16;
 }
 
