@@ -87,6 +87,26 @@ def test_graph_replay_bit_identical(kpstm_lib, device):
         assert np.array_equal(g["km"], ref["km"]) and np.array_equal(g["fold"], ref["fold"])
 
 
+def test_graph_replay_on_a_caller_stream(kpstm_lib):
+    """Graph capture and replay on the caller's stream (kpstm_set_stream):
+    the same accumulators as direct launches on the context's own stream."""
+    s = _survey(capi.MODE_FULL)
+    ref = _image(s, device=True)
+    hdr_be = np.ascontiguousarray(segy.headers_be(s.headers), dtype=np.int32)
+    dh = torch.from_numpy(hdr_be).cuda()
+    ds = torch.from_numpy(np.ascontiguousarray(s.samples)).cuda()
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with Migration(s.params, s.velocity) as m:
+        m.set_stream(stream.cuda_stream)
+        m.set_launch(graph=1)
+        for b0 in range(0, s.ntr, 250):
+            b1 = min(s.ntr, b0 + 250)
+            m.add_traces_device(dh[b0:b1].data_ptr(), ds[b0:b1].data_ptr(), b1 - b0)
+        km, fold = m.accumulators()
+    assert np.array_equal(km, ref["km"]) and np.array_equal(fold, ref["fold"])
+
+
 def test_set_launch_rejects_bad_values(kpstm_lib):
     s = _survey(capi.MODE_FULL, ntr=10)
     with Migration(s.params, s.velocity) as m:
