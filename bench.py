@@ -402,8 +402,10 @@ def run_offset_bins(args):
 def run_line(args):
     """The 2-D line: 200 CMPs x 48 offsets = 9,600 traces, 1001 samples at
     4 ms, 48 offset classes x 200 columns, reference operator (bit-exact
-    accumulators).  A step images the whole line once (1.61e9 pairs) from
-    device-resident traces."""
+    accumulators).  The launch configuration is chosen by kpstm_autotune on
+    the line itself (a fresh context), as a job loop would on its first block.
+    A step images the whole line once (1.61e9 pairs) from device-resident
+    traces."""
     import torch
     from random_gb300 import build, segy, synth
     from random_gb300.migration import Migration
@@ -415,6 +417,7 @@ def run_line(args):
     m = Migration(s.params, s.velocity)
     stream = torch.cuda.Stream(device=dev)
     m.set_stream(stream.cuda_stream)
+    cfg, tune_ms = m.autotune(d_hdr.data_ptr(), d_smp.data_ptr(), s.ntr)
 
     def step(i):
         m.add_traces_device(d_hdr.data_ptr(), d_smp.data_ptr(), s.ntr)
@@ -427,7 +430,8 @@ def run_line(args):
     line = {"workload": "line", "metric": METRIC, "value": round(pairs / elapsed / 1e9, 4), "unit": UNIT,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3),
             "dtype": "f32", "config": {"traces": int(s.ntr), "ns": 1001, "image": "200x1x48x1001",
-                                       "mode": "reference (bit-exact)"},
+                                       "mode": "reference (bit-exact)", "launch": cfg,
+                                       "autotune_ms": round(tune_ms, 3)},
             "pairs_per_step": pairs / args.steps, "clocks": clk}
     print(json.dumps(line), flush=True)
 

@@ -279,6 +279,18 @@ static int default_K(const kpstm_params *p)
     return per <= 256 ? 8 : per <= 512 ? 16 : per <= 768 ? 24 : 32;
 }
 
+/* k_prep runs one thread per trace, a sequential integral each: CTAs of 32
+   to 128 threads, so that a small block still spreads over every SM (two
+   CTAs per SM before any SM gets a third). */
+static unsigned prep_threads(const kpstm_ctx *c, int64_t ntr)
+{
+    const int64_t per = 64 * (int64_t)c->nsm;
+    int64_t w = (ntr + per - 1) / per;
+    if (w < 1) w = 1;
+    if (w > 4) w = 4;
+    return (unsigned)(32 * w);
+}
+
 /* default patch: the fewest tiles (fewest idle warps), ties to the 4 x 2
    patch, then 2 x 4, 8 x 1, 1 x 8 (4 x 2 measured fastest on the 3-D survey) */
 static int default_px(const kpstm_setup *s)
@@ -489,7 +501,8 @@ static int enqueue_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp,
     pa.tm = s->dims.trange_max;
     pa.full = p->mode == KPSTM_MODE_FULL;
     pa.dt = p->dt;
-    k_prep<<<(unsigned)((ntr + 127) / 128), 128, 0, c->cs>>>(pa);
+    const unsigned ptb = prep_threads(c, ntr);
+    k_prep<<<(unsigned)((ntr + ptb - 1) / ptb), ptb, 0, c->cs>>>(pa);
     KP_CUDA(cudaGetLastError());
     prof_end(c, pe, 1, 3);
 
@@ -1350,7 +1363,8 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
         pa.full = 1;
         pa.hilo = 1;
         pa.dt = c->p.dt;
-        k_prep<<<(unsigned)((c->lsm_nlive + 127) / 128), 128, 0, c->cs>>>(pa);
+        const unsigned ptb = prep_threads(c, c->lsm_nlive);
+        k_prep<<<(unsigned)((c->lsm_nlive + ptb - 1) / ptb), ptb, 0, c->cs>>>(pa);
         KP_CUDA(cudaGetLastError());
         KpImageArgs a = image_args(c);
         a.geom = c->d_lgeom;

@@ -301,9 +301,10 @@ __global__ void k_prep(KpPrepArgs a)
     const float dt2 = __fmul_rn(a.dt, a.dt);
     float p1 = KP_SAMPLE(0);
     float p2 = p1;
-    /* ring of P2[t-4..t] for the taps; P2[1], P2[2] kept for the mirror */
-    float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, r4 = p2;
-    float m1 = 0.f, m2 = 0.f;
+    /* ring of P2[t-4..t] for the taps (held as doubles: each float P2 value
+       is widened once, exactly); P2[1], P2[2] kept for the mirror */
+    double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0, r4 = (double)p2;
+    double m1 = 0.0, m2 = 0.0;
     for (int t = 1; t < ns + 2; ++t) {
         if (t < ns) {
             double v = __dadd_rn((double)p1, kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]));
@@ -313,13 +314,13 @@ __global__ void k_prep(KpPrepArgs a)
             p1 = __fadd_rn(p1, __fdiv_rn(flast, __fmul_rn(__fmul_rn(dt2, tf), tf)));
         }
         p2 = __fadd_rn(p2, p1);
-        if (t == 1) m1 = p2;
-        if (t == 2) m2 = p2;
-        r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = p2; /* r4 = P2[t] */
+        r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = (double)p2; /* r4 = P2[t] */
+        if (t == 1) m1 = r4;
+        if (t == 2) m2 = r4;
         if (t >= 2) {
             int T = t - 2;
-            float pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
-            double d = __dadd_rn(__dadd_rn(-2.0 * (double)r2, (double)pm), (double)r4);
+            double pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
+            double d = __dadd_rn(__dadd_rn(-2.0 * r2, pm), r4);
             if (T < ns) row[T] = __double2float_rn(d);
         }
     }
