@@ -407,13 +407,15 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     const int ns = a.ns;
     const int64_t row = a.row;
 
-    /* shared layout (lane l owns samples tw0 + l + 32k):
-       reference (two samples per packed-fp32 instruction, k = 2q and 2q + 1):
+    /* shared layout (lane l owns samples tw0 + l + 32k; both modes take two
+       samples per packed-fp32 instruction, k = 2q and 2q + 1, i.e. t and t + 32):
+       reference:
          s_v float4 [8][K/2][32] {v2(t), v2(t+32), -RN(1/v2(t)), -RN(1/v2(t+32))}
          s_t float2 [K/2][32]    {t2(t), t2(t+32)}            (t2: Kirchhoff.c:1247)
        full:
-         s_v float2 [8][W]       {(t/2)^2, 1/(v dt)^2}  (sample units: the square
-                                 roots of the DSR terms come out in samples) */
+         s_v float4 [8][K/2][32] {(t/2)^2, (t'/2)^2, 1/(v(t) dt)^2, 1/(v(t') dt)^2},
+                                 t' = t + 32 (sample units: the square roots of
+                                 the DSR terms come out in samples) */
     uint8_t *p = smem;
     float2 *s_v = reinterpret_cast<float2 *>(p);
     p += sizeof(float2) * KPSTM_COLS_PER_CTA * W;
@@ -433,11 +435,14 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     const int vrow = colok ? a.colrow[col] : -1;
     const float rdt2 = a.rdt * a.rdt;
     if (FULL) {
-        for (int t = lane; t < W; t += 32) {
-            const int tt = tw0 + t;
-            float2 v = make_float2(1.0f, 1.0f);
-            if (vrow >= 0 && tt < ns) v = a.vrows[(int64_t)vrow * ns + tt];
-            s_v[w * W + t] = make_float2(tt < ns ? a.t2c[tt].x : 1.0f, v.y * rdt2);
+        for (int i = lane; i < (K / 2) * 32; i += 32) {
+            const int q = i >> 5, l = i & 31;
+            const int ta = tw0 + l + 64 * q, tb = ta + 32;
+            float2 va = make_float2(1.0f, 1.0f), vb = make_float2(1.0f, 1.0f);
+            if (vrow >= 0 && ta < ns) va = a.vrows[(int64_t)vrow * ns + ta];
+            if (vrow >= 0 && tb < ns) vb = a.vrows[(int64_t)vrow * ns + tb];
+            reinterpret_cast<float4 *>(s_v)[(w * (K / 2) + q) * 32 + l] =
+                make_float4(ta < ns ? a.t2c[ta].x : 1.0f, tb < ns ? a.t2c[tb].x : 1.0f, va.y * rdt2, vb.y * rdt2);
         }
     } else {
         for (int i = lane; i < (K / 2) * 32; i += 32) {
@@ -605,56 +610,108 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                            accumulators are read (ts' = ts/dt) */
                         const float axs = __fmul_rn(sx, a.aax), axr = __fmul_rn(gx, a.aax);
                         const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
-                        /* q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm;
-                           the hi/lo table {hi(P(i)), lo(P(i)), P(i+1)-P(i), 0} keeps P to
-                           ~1e-14 for noisy traces (least-squares operators) */
                         /* the entry of P index floor(y) - 1 (x = y - 1 in the P index):
                            q2[i] holds {P(i), P(i+1) - P(i)} for P index i >= -tm;
                            the hi/lo table {hi(P(i)), lo(P(i)), P(i+1)-P(i), 0} keeps P to
                            ~1e-14 for noisy traces (least-squares operators) */
                         const float2 *q2 = reinterpret_cast<const float2 *>(tab) + (a.tm - 1);
                         const float4 *q4 = reinterpret_cast<const float4 *>(tab) + (a.tm - 1);
+                        const float4 *sv4 = reinterpret_cast<const float4 *>(s_v) + w * (K / 2) * 32 + lane;
+                        /* the triangle-filtered tap of one sample from the floors' bits
+                           b* and the fractions f* of y = Tf, Tf + Lf, Tf - Lf; second
+                           difference without cancellation: table differences (exact for
+                           neighbouring values) plus the interpolation terms; equals
+                           sum_k f[k] max(0, Lf - |Tf - k|) */
+                        auto tri_of = [&](int b0, int ba, int bb, float f0, float fa, float fb) -> float {
+                            if (HILO) {
+                                const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
+                                const float4 Qb = q4[bb - KP_MAGIC_BITS];
+                                const float big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
+                                return fmaf(-2.0f * f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
+                            } else {
+                                const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
+                                const float2 Qb = q2[bb - KP_MAGIC_BITS];
+                                /* each interpolation term joins the table difference of its
+                                   own tap (values of like size), the centre term last */
+                                const float ua = fmaf(fa, Qa.y, Qa.x - Q0.x), ub = fmaf(fb, Qb.y, Qb.x - Q0.x);
+                                return fmaf(-2.0f * f0, Q0.y, ua + ub);
+                            }
+                        };
+                        /* one sample alone (its pair partner lies past the trace end) */
+                        auto tap1 = [&](float Tf, float rs, float rr, float rv2, float &wgt) -> float {
+                            float Lf;
+                            kp_pair_width(rs, rr, axs, axr, ays, ayr, rv2, a.lmaxf, Lf, wgt);
+                            const float ya = Tf + Lf, yb = Tf - Lf;
+                            const int b0 = kp_floor_bits(Tf), ba = kp_floor_bits(ya), bb = kp_floor_bits(yb);
+                            return tri_of(b0, ba, bb, Tf - (__int_as_float(b0) - KP_MAGIC),
+                                          ya - (__int_as_float(ba) - KP_MAGIC), yb - (__int_as_float(bb) - KP_MAGIC));
+                        };
+                        auto add1 = [&](float &ak, float &ck, float wgt, float tri) {
+                            if (KAHAN) {
+                                const float y = fmaf(wgt, tri, -ck);
+                                const float s2 = ak + y;
+                                ck = (s2 - ak) - y;
+                                ak = s2;
+                            } else {
+                                ak = fmaf(wgt, tri, ak);
+                            }
+                        };
 #pragma unroll
-                        for (int k = 0; k < K; ++k) {
-                            const float2 tv = sv[32 * k]; /* sample tw0 + lane + 32k */
-                            float rs, rr;
-                            const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
-                            if (Tf < tmax) { /* late samples of far traces skip the taps */
-                                float Lf, wgt;
-                                kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                                const float y0 = Tf, ya = y0 + Lf, yb = y0 - Lf;
-                                const int b0 = kp_floor_bits(y0), ba = kp_floor_bits(ya), bb = kp_floor_bits(yb);
-                                const float f0 = y0 - (__int_as_float(b0) - KP_MAGIC);
-                                const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
-                                const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
-                                /* second difference without cancellation: table differences
-                                   (exact for neighbouring values) plus the interpolation terms;
-                                   equals sum_k f[k] max(0, Lf - |Tf - k|) */
-                                float tri;
-                                if (HILO) {
-                                    const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
-                                    const float4 Qb = q4[bb - KP_MAGIC_BITS];
-                                    const float big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
-                                    tri = fmaf(-2.0f * f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
-                                } else {
-                                    const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
-                                    const float2 Qb = q2[bb - KP_MAGIC_BITS];
-                                    /* each interpolation term joins the table difference of its own
-                                       tap (values of like size), the centre term last */
-                                    const float ua = fmaf(fa, Qa.y, Qa.x - Q0.x), ub = fmaf(fb, Qb.y, Qb.x - Q0.x);
-                                    tri = fmaf(-2.0f * f0, Q0.y, ua + ub);
-                                }
-                                float &ak = (k & 1) ? acc[k >> 1].y : acc[k >> 1].x;
+                        for (int q = 0; q < K / 2; ++q) {
+                            /* samples t = tw0 + lane + 64q and t + 32 as one pair: the
+                               packed operations round each half exactly as the scalar
+                               kp_pair_time / kp_pair_width do, so both paths (and the
+                               demigration) see identical pairs */
+                            const float4 vv = sv4[32 * q];
+                            const float2 tx = make_float2(vv.x, vv.y), ty = make_float2(vv.z, vv.w);
+                            const float2 as2 = __ffma2_rn(kp_bc2(dIS2), ty, tx), ar2 = __ffma2_rn(kp_bc2(dIR2), ty, tx);
+                            const float2 rs2 = make_float2(kp_rsqrt_approx(as2.x), kp_rsqrt_approx(as2.y));
+                            const float2 rr2 = make_float2(kp_rsqrt_approx(ar2.x), kp_rsqrt_approx(ar2.y));
+                            const float2 Tf2 = __ffma2_rn(as2, rs2, __fmul2_rn(ar2, rr2));
+                            const bool va = Tf2.x < tmax, vb = Tf2.y < tmax; /* late samples of far traces skip */
+                            if (va && vb) {
+                                const float2 gxx = __ffma2_rn(kp_bc2(axs), rs2, __fmul2_rn(kp_bc2(axr), rr2));
+                                const float2 gyy = __ffma2_rn(kp_bc2(ays), rs2, __fmul2_rn(kp_bc2(ayr), rr2));
+                                const float2 sg = make_float2(__fadd_rn(fabsf(gxx.x), fabsf(gyy.x)),
+                                                              __fadd_rn(fabsf(gxx.y), fabsf(gyy.y)));
+                                float2 Lf2 = __ffma2_rn(sg, ty, kp_bc2(1.0f));
+                                Lf2 = make_float2(fminf(Lf2.x, a.lmaxf), fminf(Lf2.y, a.lmaxf));
+                                const float2 ui = __fmul2_rn(__fadd2_rn(rs2, rr2),
+                                                             make_float2(kp_rcp_approx(Lf2.x), kp_rcp_approx(Lf2.y)));
+                                const float2 w2 = __fmul2_rn(ui, ui);
+                                const float2 ya2 = __fadd2_rn(Tf2, Lf2), yb2 = __fadd2_rn(Tf2, kp_neg2(Lf2));
+                                const float2 mg = kp_bc2(KP_MAGIC), nmg = kp_bc2(-KP_MAGIC);
+                                const float2 B0 = __fadd2_rz(Tf2, mg), Ba = __fadd2_rz(ya2, mg), Bb = __fadd2_rz(yb2, mg);
+                                const float2 f0 = __fadd2_rn(Tf2, kp_neg2(__fadd2_rn(B0, nmg)));
+                                const float2 fa = __fadd2_rn(ya2, kp_neg2(__fadd2_rn(Ba, nmg)));
+                                const float2 fb = __fadd2_rn(yb2, kp_neg2(__fadd2_rn(Bb, nmg)));
+                                const float2 tri2 = make_float2(
+                                    tri_of(__float_as_int(B0.x), __float_as_int(Ba.x), __float_as_int(Bb.x), f0.x, fa.x, fb.x),
+                                    tri_of(__float_as_int(B0.y), __float_as_int(Ba.y), __float_as_int(Bb.y), f0.y, fa.y, fb.y));
                                 if (KAHAN) {
-                                    float &ck = (k & 1) ? comp[k >> 1].y : comp[k >> 1].x;
-                                    float y = fmaf(wgt, tri, -ck);
-                                    float s2 = ak + y;
-                                    ck = (s2 - ak) - y;
-                                    ak = s2;
+                                    const float2 y = __ffma2_rn(w2, tri2, kp_neg2(comp[q]));
+                                    const float2 s2 = __fadd2_rn(acc[q], y);
+                                    comp[q] = __fadd2_rn(__fadd2_rn(s2, kp_neg2(acc[q])), kp_neg2(y));
+                                    acc[q] = s2;
                                 } else {
-                                    ak = fmaf(wgt, tri, ak);
+                                    acc[q] = __ffma2_rn(w2, tri2, acc[q]);
                                 }
-                                cnt[k] += 1;
+                                cnt[2 * q] += 1;
+                                cnt[2 * q + 1] += 1;
+                            } else {
+                                float &cx = comp[KAHAN ? q : 0].x, &cy = comp[KAHAN ? q : 0].y;
+                                if (va) {
+                                    float wgt;
+                                    const float tri = tap1(Tf2.x, rs2.x, rr2.x, ty.x, wgt);
+                                    add1(acc[q].x, cx, wgt, tri);
+                                    cnt[2 * q] += 1;
+                                }
+                                if (vb) {
+                                    float wgt;
+                                    const float tri = tap1(Tf2.y, rs2.y, rr2.y, ty.y, wgt);
+                                    add1(acc[q].y, cy, wgt, tri);
+                                    cnt[2 * q + 1] += 1;
+                                }
                             }
                         }
                     }
