@@ -251,13 +251,13 @@ def run_ours(args, rank, world, local_rank):
     achieved = b_alg / t_launch / 1e9
     pairs_per_launch = pairs / launches
     # DRAM traffic per launch from ncu (dram__bytes_read + write) of a
-    # 5,000-trace launch of the default kernel (3 CTAs/SM, K = 16) into the same
-    # image: 4.194e9 bytes, of which the tap tables are 5,000 rows; the
-    # accumulator part is fixed, the table part grows with the traces
-    traffic = 4.194e9 + (block - 5000) * row_floats * 4
-    # issue-slot roofline: warp instructions per pair from the same capture
-    # (56.1 per 32 pairs) against 4 schedulers x SMs x the SM clock
-    instr_per_pair = 56.1 / 32
+    # 5,000-trace launch of the default kernel (3 CTAs/SM, K = 16, persistent)
+    # into the same image: 3.944e9 bytes, of which the tap tables are 5,000
+    # rows; the accumulator part is fixed, the table part grows with the traces
+    traffic = 3.944e9 + (block - 5000) * row_floats * 4
+    # issue-slot roofline: warp instructions per pair from a capture of the same
+    # launch (37.2 per 32 pairs) against 4 schedulers x SMs x the SM clock
+    instr_per_pair = 37.23 / 32
     issue_peak = 4 * 152 * (clk.get("sm_mhz") or peaks["sm_max_mhz"]) * 1e6
     issue_achieved = pairs_per_launch / t_launch * instr_per_pair
     roofline = {
@@ -267,7 +267,8 @@ def run_ours(args, rank, world, local_rank):
         "peak_source": peaks["source"], "kernel": "k_image (full mode)",
         "algorithmic_bytes_per_launch": b_alg, "launch_ms": round(t_launch * 1e3, 3),
         "pairs_per_launch": pairs_per_launch,
-        "binding": "issue slots (no tensor work; HBM bytes per pair are ~1e-3): see profiles/",
+        "binding": "SM instruction issue and latency (no tensor work; HBM bytes per pair are ~1e-3; "
+                   "FMA, ALU and SFU pipes each at most ~55% busy): see profiles/",
         "issue": {"achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
                   "unit": "T warp-instr/s", "frac": round(issue_achieved / issue_peak, 4),
                   "instr_per_pair_source": "ncu smsp__inst_executed / pairs, 5,000-trace launch"},

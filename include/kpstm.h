@@ -222,7 +222,8 @@ typedef struct {
                              at most 16 with 3 CTAs per SM) */
     int persistent;       /* 1: one resident grid takes (class, tile, window) items
                              from a device counter, largest classes first;
-                             0: one CTA per item */
+                             0: one CTA per item.  Default: 1 for full mode
+                             with fp32 storage, else 0 */
     int graph;            /* 1: each block's device pipeline (geometry, bucketing,
                              tap tables, imaging) is captured once per block shape
                              into a CUDA graph and replayed; ignored while

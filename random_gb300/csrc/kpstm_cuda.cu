@@ -109,6 +109,7 @@ struct kpstm_ctx {
     cudaEvent_t *ev;             /* pairs: start, stop */
     int *evstage;                /* 0 image, 1 prep, 2 finish */
     int *evlaunches;
+    int64_t prof_extra;          /* launches inside image stages besides k_image (class ranking) */
 };
 
 /* Stage bracketing for kpstm_profile_*; no-ops when profiling is off. */
@@ -157,6 +158,20 @@ static float strict_bound_f(double A)
     const float f = (float)A;
     if (A != A || (double)f >= A) return f; /* exact, or f is the next float above A */
     return nextafterf(f, INFINITY);
+}
+
+/* The float X with (RN(sqrt(x)) < a) == (x < X) for every float x >= 0, so
+   that the kernels test the squared distance instead of rounding its square
+   root (RN(sqrt(.)) is monotone, so the passing x form a down-set; the float
+   square root is correctly rounded through double). */
+static float sq_bound_f(float a)
+{
+    if (!(a > 0.0f)) return 0.0f;
+    if (isinf(a)) return INFINITY;
+    float x = (float)((double)a * (double)a);
+    while (x > 0.0f && (float)sqrt((double)nextafterf(x, 0.0f)) >= a) x = nextafterf(x, 0.0f);
+    while (!isinf(x) && (float)sqrt((double)x) < a) x = nextafterf(x, INFINITY);
+    return x;
 }
 
 /* ---- imaging launch ------------------------------------------------------- */
@@ -241,6 +256,7 @@ static cudaError_t launch_image(kpstm_ctx *c, KpImageArgs a, int nclass, bool hi
         int64_t grid = (int64_t)occ * c->nsm;
         if (grid > nitems) grid = nitems;
         k_class_order<<<1, 1024, 0, c->cs>>>(a.class_start, nclass, c->d_clsorder);
+        if (c->prof) ++c->prof_extra;
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemsetAsync(c->d_queue, 0, sizeof(int), c->cs);
         if (e != cudaSuccess) return e;
@@ -585,9 +601,11 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     cudaGetDevice(&c->device);
     const int ns = params->ns, tm = s.dims.trange_max;
     const int ncol = s.ncol;
-    /* full mode with fp32 storage: the 3-CTAs-per-SM variant (K <= 16), measured
-       faster than 2 CTAs with K = 24 on the 3-D survey */
+    /* full mode with fp32 storage: the 3-CTAs-per-SM variant (K <= 16) in a
+       persistent launch, measured faster than 2 CTAs with K = 24 and than the
+       grid launch on the 3-D survey */
     c->minb = (params->mode == KPSTM_MODE_FULL && params->precision == KPSTM_PREC_FP32) ? 3 : 2;
+    c->persistent = c->minb == 3;
     set_K(c, c->minb == 3 && default_K(params) > 16 ? 16 : default_K(params));
     {
         int dev = 0;
@@ -1074,6 +1092,8 @@ extern "C" int kpstm_profile_read(kpstm_ctx *c, kpstm_profile *out)
         cudaEventDestroy(c->ev[i]);
         cudaEventDestroy(c->ev[i + 1]);
     }
+    out->other_launches += c->prof_extra;
+    c->prof_extra = 0;
     c->nev = 0;
     return KPSTM_OK;
 }
@@ -1328,6 +1348,7 @@ static KpImageArgs image_args(const kpstm_ctx *c)
     a.nsf = (float)p->ns;
     a.aperture = p->aperture;
     a.aperture_f = strict_bound_f(p->aperture);
+    a.aperture_x2 = sq_bound_f(a.aperture_f);
     float r = (float)(p->aperture * (1.0 + 1e-5) + 1e-3);
     a.tile_r2 = r * r;
     a.aax = (float)p->iline_distance;
@@ -1419,6 +1440,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     if (a.ady == 0.0f) a.ady = 1.0f;
     a.aperture = p->aperture;
     a.aperture_f = strict_bound_f(p->aperture);
+    a.aperture_x2 = sq_bound_f(a.aperture_f);
     a.tmax = (float)ns - 1.0f;
     a.lmaxf = (float)s->lmax;
     const float rdt = 1.0f / p->dt;

@@ -65,7 +65,7 @@ struct KpImageArgs {
     const float2 *t2c;             /* [ns] full mode {(t dt/2)^2, t dt/8} */
     const float *inv_l2;           /* [lmax+1] 1/L^2 */
     float *km;                     /* [ncls][ncol][ns] */
-    float *kc;                     /* Kahan compensation, same layout, or null */
+    float *kc;                     /* Kahan compensation, negated (-c), same layout, or null */
     int32_t *cnt;                  /* [ncls][ncol][ns] fold - 1 */
     unsigned long long *hits;      /* (trace, column) pairs in aperture */
     int *status;
@@ -73,6 +73,7 @@ struct KpImageArgs {
     float dt, rdt, nsf, lmaxf;
     double aperture;
     float aperture_f;              /* float x: x < aperture_f exactly when (double)x < aperture */
+    float aperture_x2;             /* float X: RN(sqrt(x)) < aperture_f exactly when x < X (x >= 0) */
     float tile_r2;                 /* squared tile-test radius (aperture + margin) */
     float aax, aay;                /* full mode: line spacings */
     const int32_t *tilecols;       /* [ntile][8] column of each warp, -1 = none */
@@ -464,9 +465,12 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     const int64_t obase = ((int64_t)cls * a.ncol + (colok ? col : 0)) * ns + tw0 + lane;
 
     /* accumulators as sample pairs: acc[q] = samples 2q (x) and 2q + 1 (y), i.e.
-       tw0 + lane + 64q and + 32 */
+       tw0 + lane + 64q and + 32; comp[q] the negated Kahan compensations (so
+       that no update needs a negation); cnt2[q] the pair's fold increments as
+       two 16-bit halves (x low, y high), added to the global counts before
+       they can overflow */
     float2 acc[K / 2], comp[KAHAN ? K / 2 : 1];
-    int cnt[K];
+    uint32_t cnt2[K / 2];
 #pragma unroll
     for (int q = 0; q < K / 2; ++q) {
         const int ta = tw0 + lane + 64 * q, tb = ta + 32;
@@ -476,9 +480,18 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
             comp[q].x = (colok && ta < ns) ? a.kc[obase + 64 * q] : 0.0f;
             comp[q].y = (colok && tb < ns) ? a.kc[obase + 64 * q + 32] : 0.0f;
         }
-        cnt[2 * q] = 0;
-        cnt[2 * q + 1] = 0;
+        cnt2[q] = 0u;
     }
+    auto flush_counts = [&]() {
+        if (!colok) return;
+#pragma unroll
+        for (int q = 0; q < K / 2; ++q) {
+            const int ta = tw0 + lane + 64 * q, tb = ta + 32;
+            if (ta < ns) a.cnt[obase + 64 * q] += (int32_t)(cnt2[q] & 0xffffu);
+            if (tb < ns) a.cnt[obase + 64 * q + 32] += (int32_t)(cnt2[q] >> 16);
+            cnt2[q] = 0u;
+        }
+    };
     __syncthreads();
 
     const int cb = a.class_start[cls], ce = a.class_start[cls + 1];
@@ -548,13 +561,17 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                     g.cmpx = g1.x;
                     g.cmpy = g1.y;
                     float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
-                    float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-                    if (!(dIC < a.aperture_f)) break; /* Kirchhoff.c:1352-1354, warp-uniform */
+                    /* RN(sqrt(dIC2)) < aperture_f, decided on the square (Kirchhoff.c:1352-1354),
+                       warp-uniform */
+                    const float dIC2 = __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy));
+                    if (!(dIC2 < a.aperture_x2)) break;
                     if (vrow < 0) {
                         kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
                         break;
                     }
-                    ++my_hits;
+                    /* every 32,768 hits the 16-bit counts go to the global ones
+                       (warp-uniform: the aperture test is) */
+                    if ((++my_hits & 0x7fff) == 0) flush_counts();
                     float sx = __fsub_rn(IX, g.sxt), sy = __fsub_rn(IY, g.syt);
                     float gx = __fsub_rn(IX, g.gxt), gy = __fsub_rn(IY, g.gyt);
                     const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
@@ -588,16 +605,15 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                             const int ia = va ? (int)((uint32_t)__float_as_int(fb.x) - 0xCB400000u) : ns;
                             const int ib = vb ? (int)((uint32_t)__float_as_int(fb.y) - 0xCB400000u) : ns;
                             const float2 d = make_float2(tab[ia], tab[ib]);
-                            if (KAHAN) {
-                                const float2 y = __fadd2_rn(d, kp_neg2(comp[q]));
+                            if (KAHAN) { /* comp = -c: y = d - c, -c' = y - (s - acc) */
+                                const float2 y = __fadd2_rn(d, comp[q]);
                                 const float2 s = __fadd2_rn(acc[q], y);
-                                comp[q] = __fadd2_rn(__fadd2_rn(s, kp_neg2(acc[q])), kp_neg2(y));
+                                comp[q] = kp_sub2(y, kp_sub2(s, acc[q]));
                                 acc[q] = s;
                             } else {
                                 acc[q] = __fadd2_rn(acc[q], d); /* + 0 where T >= ns: exact no-op */
                             }
-                            cnt[2 * q] += va;
-                            cnt[2 * q + 1] += vb;
+                            cnt2[q] += (uint32_t)va | ((uint32_t)vb << 16);
                         }
                     } else {
                         /* full physics in sample units: a = (t/2)^2 + |I-S|^2/(v dt)^2,
@@ -622,19 +638,20 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                            difference without cancellation: table differences (exact for
                            neighbouring values) plus the interpolation terms; equals
                            sum_k f[k] max(0, Lf - |Tf - k|) */
-                        auto tri_of = [&](int b0, int ba, int bb, float f0, float fa, float fb) -> float {
+                        auto tri_of = [&](int b0, int ba, int bb, float m2f0, float fa, float fb) -> float {
+                            /* m2f0 = -2 f0 */
                             if (HILO) {
                                 const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
                                 const float4 Qb = q4[bb - KP_MAGIC_BITS];
                                 const float big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
-                                return fmaf(-2.0f * f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
+                                return fmaf(m2f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
                             } else {
                                 const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
                                 const float2 Qb = q2[bb - KP_MAGIC_BITS];
                                 /* each interpolation term joins the table difference of its
                                    own tap (values of like size), the centre term last */
                                 const float ua = fmaf(fa, Qa.y, Qa.x - Q0.x), ub = fmaf(fb, Qb.y, Qb.x - Q0.x);
-                                return fmaf(-2.0f * f0, Q0.y, ua + ub);
+                                return fmaf(m2f0, Q0.y, ua + ub);
                             }
                         };
                         /* one sample alone (its pair partner lies past the trace end) */
@@ -643,14 +660,14 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                             kp_pair_width(rs, rr, axs, axr, ays, ayr, rv2, a.lmaxf, Lf, wgt);
                             const float ya = Tf + Lf, yb = Tf - Lf;
                             const int b0 = kp_floor_bits(Tf), ba = kp_floor_bits(ya), bb = kp_floor_bits(yb);
-                            return tri_of(b0, ba, bb, Tf - (__int_as_float(b0) - KP_MAGIC),
+                            return tri_of(b0, ba, bb, -2.0f * (Tf - (__int_as_float(b0) - KP_MAGIC)),
                                           ya - (__int_as_float(ba) - KP_MAGIC), yb - (__int_as_float(bb) - KP_MAGIC));
                         };
-                        auto add1 = [&](float &ak, float &ck, float wgt, float tri) {
-                            if (KAHAN) {
-                                const float y = fmaf(wgt, tri, -ck);
+                        auto add1 = [&](float &ak, float &nck, float wgt, float tri) {
+                            if (KAHAN) { /* nck = -c */
+                                const float y = fmaf(wgt, tri, nck);
                                 const float s2 = ak + y;
-                                ck = (s2 - ak) - y;
+                                nck = y - (s2 - ak);
                                 ak = s2;
                             } else {
                                 ak = fmaf(wgt, tri, ak);
@@ -679,38 +696,41 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 const float2 ui = __fmul2_rn(__fadd2_rn(rs2, rr2),
                                                              make_float2(kp_rcp_approx(Lf2.x), kp_rcp_approx(Lf2.y)));
                                 const float2 w2 = __fmul2_rn(ui, ui);
-                                const float2 ya2 = __fadd2_rn(Tf2, Lf2), yb2 = __fadd2_rn(Tf2, kp_neg2(Lf2));
-                                const float2 mg = kp_bc2(KP_MAGIC), nmg = kp_bc2(-KP_MAGIC);
+                                const float2 ya2 = __fadd2_rn(Tf2, Lf2), yb2 = kp_sub2(Tf2, Lf2);
+                                const float2 mg = kp_bc2(KP_MAGIC);
                                 const float2 B0 = __fadd2_rz(Tf2, mg), Ba = __fadd2_rz(ya2, mg), Bb = __fadd2_rz(yb2, mg);
-                                const float2 f0 = __fadd2_rn(Tf2, kp_neg2(__fadd2_rn(B0, nmg)));
-                                const float2 fa = __fadd2_rn(ya2, kp_neg2(__fadd2_rn(Ba, nmg)));
-                                const float2 fb = __fadd2_rn(yb2, kp_neg2(__fadd2_rn(Bb, nmg)));
+                                /* fractions y - floor(y), with M - B = -floor(y) exactly */
+                                const float2 fa = __fadd2_rn(ya2, kp_sub2(mg, Ba));
+                                const float2 fb = __fadd2_rn(yb2, kp_sub2(mg, Bb));
+                                /* -2 f0 = 2 floor(Tf) - 2 Tf: 2 B0 - 2M is exact, and so is
+                                   -2 (Tf - floor(Tf)) for Tf >= 0 (one rounding of an exact value) */
+                                const float2 m2f0 = __ffma2_rn(Tf2, kp_bc2(-2.0f),
+                                                               __ffma2_rn(B0, kp_bc2(2.0f), kp_bc2(-2.0f * KP_MAGIC)));
                                 const float2 tri2 = make_float2(
-                                    tri_of(__float_as_int(B0.x), __float_as_int(Ba.x), __float_as_int(Bb.x), f0.x, fa.x, fb.x),
-                                    tri_of(__float_as_int(B0.y), __float_as_int(Ba.y), __float_as_int(Bb.y), f0.y, fa.y, fb.y));
-                                if (KAHAN) {
-                                    const float2 y = __ffma2_rn(w2, tri2, kp_neg2(comp[q]));
+                                    tri_of(__float_as_int(B0.x), __float_as_int(Ba.x), __float_as_int(Bb.x), m2f0.x, fa.x, fb.x),
+                                    tri_of(__float_as_int(B0.y), __float_as_int(Ba.y), __float_as_int(Bb.y), m2f0.y, fa.y, fb.y));
+                                if (KAHAN) { /* comp = -c: y = w tri - c, -c' = y - (s - acc) */
+                                    const float2 y = __ffma2_rn(w2, tri2, comp[q]);
                                     const float2 s2 = __fadd2_rn(acc[q], y);
-                                    comp[q] = __fadd2_rn(__fadd2_rn(s2, kp_neg2(acc[q])), kp_neg2(y));
+                                    comp[q] = kp_sub2(y, kp_sub2(s2, acc[q]));
                                     acc[q] = s2;
                                 } else {
                                     acc[q] = __ffma2_rn(w2, tri2, acc[q]);
                                 }
-                                cnt[2 * q] += 1;
-                                cnt[2 * q + 1] += 1;
+                                cnt2[q] += 0x00010001u;
                             } else {
                                 float &cx = comp[KAHAN ? q : 0].x, &cy = comp[KAHAN ? q : 0].y;
                                 if (va) {
                                     float wgt;
                                     const float tri = tap1(Tf2.x, rs2.x, rr2.x, ty.x, wgt);
                                     add1(acc[q].x, cx, wgt, tri);
-                                    cnt[2 * q] += 1;
+                                    cnt2[q] += 1u;
                                 }
                                 if (vb) {
                                     float wgt;
                                     const float tri = tap1(Tf2.y, rs2.y, rr2.y, ty.y, wgt);
                                     add1(acc[q].y, cy, wgt, tri);
-                                    cnt[2 * q + 1] += 1;
+                                    cnt2[q] += 0x00010000u;
                                 }
                             }
                         }
@@ -746,15 +766,14 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
             if (ta < ns) {
                 a.km[obase + 64 * q] = acc[q].x;
                 if (KAHAN) a.kc[obase + 64 * q] = comp[q].x;
-                a.cnt[obase + 64 * q] += cnt[2 * q];
             }
             if (tb < ns) {
                 a.km[obase + 64 * q + 32] = acc[q].y;
                 if (KAHAN) a.kc[obase + 64 * q + 32] = comp[q].y;
-                a.cnt[obase + 64 * q + 32] += cnt[2 * q + 1];
             }
         }
     }
+    flush_counts();
     if (win == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
     return true;
 }
@@ -824,6 +843,7 @@ struct KpDemigArgs {
     float ax0, adx, ay0, ady;      /* column coordinates: IX(xc) ~ ax0 + xc adx */
     double aperture;
     float aperture_f;              /* as KpImageArgs */
+    float aperture_x2;             /* as KpImageArgs */
     float tmax, lmaxf, rdt2, aax, aay, dt;
 };
 
@@ -949,8 +969,8 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
             const float2 cxy = a.colxy[col];
             const float IX = cxy.x, IY = cxy.y;
             float cx = __fsub_rn(IX, g.cmpx), cy = __fsub_rn(IY, g.cmpy);
-            float dIC = __fsqrt_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-            if (!(dIC < a.aperture_f)) continue;
+            const float dIC2 = __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy));
+            if (!(dIC2 < a.aperture_x2)) continue; /* RN(sqrt(dIC2)) < aperture_f, as k_image */
             const int vrow = a.colrow[col];
             if (vrow < 0) {
                 kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
