@@ -89,3 +89,17 @@ def test_trilinear_velocity_matches_fp64_oracle(kpstm_lib, oracle_lib):
     assert rel_l2(g["km"], o["km"]) <= ACC_TOL, rel_l2(g["km"], o["km"])
     near = migrate(s, want_acc=True)
     assert rel_l2(near["km"], g["km"]) > 10 * ACC_TOL
+
+
+def test_fold_counts_beyond_16_bits(kpstm_lib):
+    """Full mode, stack output, 40,000 traces (a 400-trace survey repeated) in
+    one block: every column's work item sees more hits than the kernel's 16-bit
+    per-sample fold counters hold; the one-block result equals the one from
+    3,000-trace blocks (where no item gets that far) bit for bit."""
+    import dataclasses
+    s = _survey(nx=4, ny=2, nh=1, dh=1e9, output=capi.OUT_STACK)
+    s = dataclasses.replace(s, headers=np.tile(s.headers, (100, 1)), samples=np.tile(s.samples, (100, 1)))
+    a = migrate(s, block=s.ntr, want_acc=True)
+    b = migrate(s, block=3000, want_acc=True)
+    assert int(a["fold"].max()) > 32_768
+    assert np.array_equal(a["km"], b["km"]) and np.array_equal(a["fold"], b["fold"])
