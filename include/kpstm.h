@@ -228,11 +228,13 @@ typedef struct {
                              tap tables, imaging) is captured once per block shape
                              into a CUDA graph and replayed; ignored while
                              profiling is enabled */
-    int ctas_per_sm;      /* imaging kernel variant: 2 or 3 resident CTAs per SM -
+    int ctas_per_sm;      /* imaging kernel variant: 2, 3 or 4 resident CTAs per SM -
                              3 trades register space (80 per thread, so
                              samples_per_lane <= 16 in full mode, <= 8 with
                              Kahan sums or in reference mode) and pipeline
-                             depth for 24 resident warps; 0 = default (3 for
+                             depth for 24 resident warps; 4 (64 registers,
+                             32 warps) exists for full mode with fp32 storage
+                             and samples_per_lane = 8 only; 0 = default (3 for
                              full mode with fp32 storage, else 2) */
     int reserved[3];
 } kpstm_launch;

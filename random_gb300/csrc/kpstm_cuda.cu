@@ -46,7 +46,7 @@ struct kpstm_ctx {
     int64_t ntile;               /* image tiles of 8 columns */
     int tile_px;                 /* tile patch: tile_px x (8 / tile_px) columns */
     int persistent, use_graph;   /* launch configuration (kpstm_launch) */
-    int minb;                    /* imaging CTAs per SM the kernel variant is built for: 2 or 3 */
+    int minb;                    /* imaging CTAs per SM the kernel variant is built for: 2, 3 or 4 */
     int dirty;                   /* traces imaged since create / reset */
     int nsm;                     /* multiprocessors of the device */
     int64_t row;                 /* floats per tap-table row */
@@ -209,6 +209,10 @@ static kp_image_fn image_fn_k(bool full, bool kahan, bool hilo, int minb)
     }
     if (full && minb == 3) {
         if constexpr (K <= 16) return k_image<K, true, false, false, 3>;
+        return nullptr;
+    }
+    if (full && minb == 4) {
+        if constexpr (K <= 8) return k_image<K, true, false, false, 4>;
         return nullptr;
     }
     if (full) {
@@ -1130,8 +1134,10 @@ extern "C" int kpstm_set_launch(kpstm_ctx *c, const kpstm_launch *cfg)
     if ((px != 1 && px != 2 && px != 4 && px != 8) || !valid_K(c, K)) return KPSTM_ERR_INVALID_ARG;
     if ((cfg->persistent != 0 && cfg->persistent != 1) || (cfg->graph != 0 && cfg->graph != 1))
         return KPSTM_ERR_INVALID_ARG;
-    if (minb != 2 && minb != 3) return KPSTM_ERR_INVALID_ARG;
+    if (minb == 4 && !cfg->samples_per_lane) K = 8;
+    if (minb != 2 && minb != 3 && minb != 4) return KPSTM_ERR_INVALID_ARG;
     if (minb == 3 && K > kmax3) return KPSTM_ERR_INVALID_ARG;
+    if (minb == 4 && (!occ3 || K > 8)) return KPSTM_ERR_INVALID_ARG; /* full mode, fp32, K = 8 only */
     drop_graphs(c);
     if (px != c->tile_px) {
         int st = set_tiles(c, px);
@@ -1171,9 +1177,11 @@ extern "C" int kpstm_autotune(kpstm_ctx *c, const int32_t *d_hdr_be, const float
         if (n > 2 * nmin) continue;
         for (int K = 8; K <= 32 && !st; K += 8) {
             if (!valid_K(c, K)) continue;
-            for (int v = 0; v < 4 && !st; ++v) {
+            for (int v = 0; v < 6 && !st; ++v) {
                 const int pers = v & 1, minb = 2 + (v >> 1);
                 if (minb == 3 && K > occ3_kmax(&c->p)) continue;
+                if (minb == 4 && (K > 8 || c->p.mode != KPSTM_MODE_FULL || c->p.precision != KPSTM_PREC_FP32))
+                    continue;
                 kpstm_launch cfg;
                 memset(&cfg, 0, sizeof(cfg));
                 cfg.tile_px = px;

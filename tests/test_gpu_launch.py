@@ -64,8 +64,11 @@ def test_launch_configs_bit_identical(kpstm_lib, mode, prec):
     prm = dict(precision=prec)
     ref = _image(s, prm)
     assert ref["pairs"] > 0
-    for px, K, pers, ctas in itertools.product((1, 2, 4, 8), _valid_K(mode, prec), (0, 1), (2, 3)):
-        if ctas == 3 and K > (16 if (mode == capi.MODE_FULL and prec == capi.PREC_FP32) else 8):
+    full32 = mode == capi.MODE_FULL and prec == capi.PREC_FP32
+    for px, K, pers, ctas in itertools.product((1, 2, 4, 8), _valid_K(mode, prec), (0, 1), (2, 3, 4)):
+        if ctas == 3 and K > (16 if full32 else 8):
+            continue
+        if ctas == 4 and (not full32 or K > 8):
             continue
         g = _image(s, prm, dict(tile_px=px, samples_per_lane=K, persistent=pers, ctas_per_sm=ctas))
         assert g["cfg"]["tile_px"] == px and g["cfg"]["samples_per_lane"] == K
@@ -111,7 +114,8 @@ def test_set_launch_rejects_bad_values(kpstm_lib):
     s = _survey(capi.MODE_FULL, ntr=10)
     with Migration(s.params, s.velocity) as m:
         for bad in (dict(tile_px=3), dict(samples_per_lane=32), dict(samples_per_lane=12), dict(persistent=2),
-                    dict(graph=-1), dict(ctas_per_sm=4), dict(ctas_per_sm=3, samples_per_lane=24)):
+                    dict(graph=-1), dict(ctas_per_sm=5), dict(ctas_per_sm=3, samples_per_lane=24),
+                    dict(ctas_per_sm=4, samples_per_lane=16)):
             with pytest.raises(capi.KpstmError) as e:
                 m.set_launch(**bad)
             assert e.value.status == 1  # KPSTM_ERR_INVALID_ARG
