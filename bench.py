@@ -517,7 +517,62 @@ def run_lsm(args):
         line["cg"] = {"iterations": args.cg_iters, "seconds": round(secs, 3),
                       "applications": 2 * args.cg_iters + 1,
                       "residual_rel": [round(float(r / resid[0]), 6) for r in resid]}
+    if args.lsm_accuracy > 0:
+        line["lsm_accuracy"] = _lsm_accuracy(args, mdl, m, stream, dev)
     print(json.dumps(line), flush=True)
+
+
+def _lsm_accuracy(args, mdl, m16, stream, dev):
+    """BF16-stored least-squares migration against FP32-stored CGLS of the
+    same data (FP64 dot products and step lengths in both; the FP32 solver
+    matches the FP64 oracle's CGLS to ~1e-6 relative where the oracle runs),
+    and the wall time of each against one plain FP32 migration of the same
+    survey (full mode: ingest, tap tables, imaging, finishing).  CGLS starts
+    from m = 0, so the iterate after k iterations comes from a k-iteration
+    run: each k is timed on its own."""
+    import numpy as np
+    import torch
+    from random_gb300 import capi, segy, synth
+    from random_gb300.migration import Migration
+    s = mdl.survey
+    d_obs = synth.synthesize_torch(mdl, device=dev)
+    m32 = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
+    m32.set_stream(stream.cuda_stream)
+    m32.lsm_geometry(s.headers)
+    x16 = torch.empty(*m16.shape, device=dev)
+    x32 = torch.empty_like(x16)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    # plain FP32 migration of the same traces (second of two runs)
+    mp = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
+    mp.set_stream(stream.cuda_stream)
+    hdr_be = torch.from_numpy(np.ascontiguousarray(segy.headers_be(s.headers), dtype=np.int32)).to(dev)
+    img = torch.empty(*mp.shape, device=dev)
+    t_plain = 0.0
+    for _ in range(2):
+        mp.reset()
+        t_plain = timed(lambda: (mp.add_traces_device(hdr_be.data_ptr(), d_obs.data_ptr(), s.ntr),
+                                 mp.finish_device(img.data_ptr())))
+    err, t16, t32 = [], [], []
+    for k in range(1, args.lsm_accuracy + 1):
+        t16.append(timed(lambda: m16.lsm_cg(d_obs.data_ptr(), k, x16.data_ptr())))
+        t32.append(timed(lambda: m32.lsm_cg(d_obs.data_ptr(), k, x32.data_ptr())))
+        err.append(float((x16.double() - x32.double()).norm() / x32.double().norm()))
+    hit = next((k + 1 for k, e in enumerate(err) if e <= 1e-3), None)
+    return {"reference": "FP32-stored CGLS, FP64 scalars", "iterations": list(range(1, args.lsm_accuracy + 1)),
+            "rel_l2_bf16_vs_fp32": [round(e, 7) for e in err],
+            "bf16_seconds": [round(t, 3) for t in t16], "fp32_seconds": [round(t, 3) for t in t32],
+            "plain_fp32_migration_seconds": round(t_plain, 3),
+            "bf16_seconds_over_plain": [round(t / t_plain, 3) for t in t16],
+            "last_iteration_within_1e-3": max([k + 1 for k, e in enumerate(err) if e <= 1e-3], default=None),
+            "first_iteration_within_1e-3": hit}
 
 
 # ----------------------------------------------------------- reference arm
@@ -563,6 +618,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cg-iters", type=int, default=0, help="lsm workload: also time this many CG iterations")
     ap.add_argument("--dot-test", action="store_true", help="lsm workload: also run the dot-product test")
+    ap.add_argument("--lsm-accuracy", type=int, default=0,
+                    help="lsm workload: BF16 vs FP32 CGLS iterates and times for 1..N iterations, "
+                         "against one plain FP32 migration of the same survey")
     ap.add_argument("--autotune", type=int, default=0,
                     help="survey workload: autotune the launch on this many traces before timing (0: default launch)")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
