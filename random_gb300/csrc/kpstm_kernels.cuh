@@ -577,7 +577,6 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                     const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
                     const float dIR2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
                     const float *tab = hdr + KP_ROW_HDR;
-                    const float2 *sv = s_v + w * W + lane;
                     if (!FULL) {
                         const float4 *sv4 = reinterpret_cast<const float4 *>(s_v) + w * (K / 2) * 32 + lane;
                         const float2 *st2 = reinterpret_cast<const float2 *>(s_t) + lane;
