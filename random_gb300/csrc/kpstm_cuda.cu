@@ -1463,10 +1463,13 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.shift = cover > 8589934592.0 ? (int)ceil(log2(cover / 8589934592.0)) : 0;
     a.absmax = c->d_absmax;
     a.order = c->d_dorder;
-    const size_t smem = sizeof(float) * 2 * (size_t)ns;
+    /* accumulator rows in shared memory when four of them fit with room for
+       several CTAs per SM, else in L2 */
+    const bool use_sh = kp_demig_smem(ns, a.ng, true) <= 48 * 1024;
+    const size_t smem = kp_demig_smem(ns, a.ng, use_sh);
     if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
     const size_t accb = sizeof(unsigned long long) * (size_t)a.ng * (size_t)c->lsm_nlive;
-    if (!c->d_dacc) {
+    if (!c->d_dacc && !use_sh) {
         if (cudaMalloc(&c->d_dacc, accb) != cudaSuccess) return KPSTM_ERR_OUT_OF_MEMORY;
     }
     if (!c->d_rvdt) {
@@ -1477,26 +1480,27 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
         KP_CUDA(cudaGetLastError());
     }
     a.rvdt = c->d_rvdt;
-    a.acc = c->d_dacc;
-    KP_CUDA(cudaFuncSetAttribute(k_demig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    a.acc = use_sh ? nullptr : c->d_dacc;
+    void (*dm)(KpDemigArgs) = use_sh ? k_demig<true> : k_demig<false>;
+    KP_CUDA(cudaFuncSetAttribute(dm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned nblk = (unsigned)((c->lsm_nlive + KP_DM_WARPS - 1) / KP_DM_WARPS);
     if (!c->dbound_ok) {
         /* once per geometry: max_k (L 1)[trace, k], the fixed-point range of each trace */
         KpDemigArgs b = a;
         b.model = nullptr;
         b.dbound_out = c->d_dbound;
-        KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
-        k_demig<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
+        if (!use_sh) KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
+        dm<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
         KP_CUDA(cudaGetLastError());
         c->dbound_ok = 1;
     }
-    KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
+    if (!use_sh) KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
     a.dbound = c->d_dbound;
     const int64_t nmodel = (int64_t)s->nclass * s->ncol * ns;
     KP_CUDA(cudaMemsetAsync(c->d_absmax, 0, sizeof(unsigned int), c->cs));
     k_absmax<<<4 * c->nsm, 256, 0, c->cs>>>(d_model, nmodel, c->d_absmax);
     KP_CUDA(cudaGetLastError());
-    k_demig<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(a);
+    dm<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(a);
     KP_CUDA(cudaGetLastError());
     return KPSTM_OK;
 }

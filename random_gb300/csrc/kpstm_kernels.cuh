@@ -878,12 +878,41 @@ __device__ __forceinline__ void kp_red_add_u64(unsigned long long *p, unsigned l
 
 #define KP_DM_NONE (-(1 << 29)) /* entry index of a lane without a pair */
 
+/* Exact 64-bit add in shared memory from two native 32-bit shared atomics:
+   the low word's add returns the word before it, which tells whether this
+   add carried out of it; the high word receives the high half plus that
+   carry.  Concurrent adds to one entry each see their own predecessor, so
+   the pair of words always holds the exact sum modulo 2^64. */
+__device__ __forceinline__ void kp_sadd_u64(unsigned long long *p, unsigned long long v)
+{
+    unsigned int *wd = reinterpret_cast<unsigned int *>(p); /* [0] low word, [1] high word */
+    const unsigned int lo = (unsigned int)v, hi = (unsigned int)(v >> 32);
+    const unsigned int old = atomicAdd(&wd[0], lo);
+    atomicAdd(&wd[1], hi + (old + lo < old ? 1u : 0u));
+}
+
+/* RN(x) as an int64 for |x| <= 2^45 with fp32 and integer operations only
+   (__float2ll_rn runs on the FP64 pipe, slow on this GPU): x = qh 2^23 + r
+   exactly with qh = RN(x 2^-23) and |r| <= 2^22; both roundings are the
+   1.5 * 2^23 shift (a float add whose spacing there is 1, ties to even), and
+   qh 2^23 is even, so the sum rounds x exactly as __float2ll_rn does. */
+__device__ __forceinline__ long long kp_f2ll_rn45(float x)
+{
+    const float sh = __fadd_rn(__fmul_rn(x, 0x1p-23f), KP_MAGIC);
+    const int qh = __float_as_int(sh) - KP_MAGIC_BITS;
+    const float r = __fmaf_rn(__fadd_rn(sh, -KP_MAGIC), -0x1p23f, x); /* x - qh 2^23, exact */
+    const int ql = __float_as_int(__fadd_rn(r, KP_MAGIC)) - KP_MAGIC_BITS;
+    return (long long)qh * 8388608LL + (long long)ql;
+}
+
 /* One tap of the transpose for the 32 lanes of a warp (consecutive samples):
    e0 at entry n, e1 at n + 1 (entries < 0 dropped).  Where the next lane's
    n is this lane's n + 1 - the usual case, the traveltime advancing by about
    a sample per sample - this lane's e1 is handed to it with a shuffle and
-   added to its e0, so one 64-bit RED per lane and tap reaches L2 instead of
-   two.  All lanes must call it. */
+   added to its e0, so one 64-bit add per lane and tap is issued instead of
+   two.  All lanes must call it.  SH: G is the warp's row in shared memory
+   (kp_sadd_u64), else the trace's row in global memory (RED to L2). */
+template <bool SH>
 __device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long long e0, long long e1, int lane)
 {
     const int np = __shfl_up_sync(0xffffffffu, n, 1);
@@ -891,8 +920,21 @@ __device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long 
     const int nn = __shfl_down_sync(0xffffffffu, n, 1);
     if (lane > 0 && np + 1 == n) e0 += e1p;         /* the previous lane's e1 lands here */
     const bool keep1 = !(lane < 31 && nn == n + 1); /* else the next lane takes it */
-    if (n >= 0) kp_red_add_u64(&G[n], (unsigned long long)e0);
-    if (keep1 && n >= -1) kp_red_add_u64(&G[n + 1], (unsigned long long)e1);
+    if (SH) {
+        if (n >= 0) kp_sadd_u64(&G[n], (unsigned long long)e0);
+        if (keep1 && n >= -1) kp_sadd_u64(&G[n + 1], (unsigned long long)e1);
+    } else {
+        if (n >= 0) kp_red_add_u64(&G[n], (unsigned long long)e0);
+        if (keep1 && n >= -1) kp_red_add_u64(&G[n + 1], (unsigned long long)e1);
+    }
+}
+
+/* Dynamic shared memory of k_demig: t2[ns] and ts[ns], then (SH) one 64-bit
+   accumulator row of ngp = ng rounded up to even entries per warp. */
+__host__ __device__ inline size_t kp_demig_smem(int ns, int ng, bool sh)
+{
+    const size_t head = sizeof(float) * 2 * (size_t)((ns + 1) & ~1);
+    return head + (sh ? (size_t)KP_DM_WARPS * (size_t)((ng + 1) & ~1) * sizeof(unsigned long long) : 0);
 }
 
 /* Demigration d = L m, the exact transpose of the full-mode migration of
@@ -912,20 +954,28 @@ __device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long 
    coefficients); (L 1) per trace comes from a bound pass of this kernel on
    the all-ones model with the conservative scale |gs| < 2^30 (weight x
    t/(8 dt) <= 2/dt).  The result is deterministic.
-   The entries are added with fire-and-forget 64-bit atomics (RED) into the
+   SH (the row fits in shared memory): each warp accumulates its trace in
+   its own 64-bit row in shared memory with exact two-word shared atomics
+   (kp_sadd_u64) and takes the prefix sums there; L2 sees no atomics.  Else
+   the entries are added with fire-and-forget 64-bit atomics (RED) into the
    trace's row in global memory, which stays in L2 while the warp works on
-   it; the prefix sums run in shared memory. */
-__global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
+   it.  The float -> int64 roundings use kp_f2ll_rn45 (no FP64 pipe); the
+   scale keeps their arguments below 2^45. */
+template <bool SH>
+__global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigArgs a)
 {
     extern __shared__ __align__(16) float dm_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ns = a.ns, ng = a.ng;
+    const int ns = a.ns, ng = a.ng, ngp = (ng + 1) & ~1;
     float *s_t2 = dm_smem;      /* [ns] (t/2)^2 */
     float *s_ts = dm_smem + ns; /* [ns] t/(8 dt) */
+    unsigned long long *s_rows = reinterpret_cast<unsigned long long *>(dm_smem + ((ns + 1) & ~1) * 2);
     for (int k = threadIdx.x; k < ns; k += blockDim.x) {
         s_t2[k] = a.t2c[k].x;
         s_ts[k] = a.tscale[k];
     }
+    if (SH)
+        for (int i = lane; i < ngp; i += 32) s_rows[(size_t)w * ngp + i] = 0ull;
     __syncthreads();
     const bool bound = a.model == nullptr;
     const unsigned int mb = bound ? __float_as_uint(1.0f) : *a.absmax;
@@ -942,9 +992,11 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
     if (bound) {
         E = 29 - (ilogbf(bw) + 1) - a.shift; /* |gs| < 2^30 */
     } else {
-        /* 2^E max|m| max(2 (L 1), 2 bw) < 2^61 */
+        /* 2^E max|m| max(2 (L 1), 2 bw) < 2^61, and |2 gs| <= 2 bw max|m| 2^E < 2^45
+           for kp_f2ll_rn45 */
         const float v = __uint_as_float(mb) * fmaxf(2.0f * a.dbound[slot], 2.0f * bw);
-        E = 61 - (ilogbf(fminf(v, 3.0e38f)) + 1);
+        E = min(61 - (ilogbf(fminf(v, 3.0e38f)) + 1),
+                43 - ilogbf(fminf(__uint_as_float(mb) * bw, 3.0e38f)));
     }
     E = max(-126, min(127, E));
     const float scale = __int_as_float((E + 127) << 23);
@@ -952,7 +1004,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
 
     const kpstm_geom g = a.geom[slot];
     const int cls = g.cls;
-    unsigned long long *Gg = a.acc + (int64_t)slot * ng;
+    unsigned long long *Gg = SH ? s_rows + (size_t)w * ngp : a.acc + (int64_t)slot * ng;
     const float apm = (float)a.aperture * 1.00001f + 1.0f; /* range margin; exact test below */
     const int x_lo = max(0, (int)floorf((g.cmpx - apm - a.ax0) / a.adx) - 1);
     const int x_hi = min(a.nx - 1, (int)ceilf((g.cmpx + apm - a.ax0) / a.adx) + 1);
@@ -1004,7 +1056,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
                     float Lf, wgt;
                     kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
                     const float gs = ok ? __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u])), scale) : 0.0f;
-                    const long long Q = __float2ll_rn(gs);
+                    const long long Q = kp_f2ll_rn45(gs);
                     /* the positions exactly as k_image computes them: y = Tf, Tf +- Lf,
                        P index n = floor(y) - 1, fraction y - floor(y) */
                     const float y0 = ok ? Tf : 1.0f, ya = y0 + Lf, yb = y0 - Lf;
@@ -1012,26 +1064,35 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
                     const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
                     const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
                     const float f0 = y0 - (__int_as_float(b00) - KP_MAGIC);
-                    const long long a1 = __float2ll_rn(__fmul_rn(gs, fa));
-                    const long long b1 = __float2ll_rn(__fmul_rn(gs, fb));
-                    const long long c1 = __float2ll_rn(__fmul_rn(-2.0f * gs, f0));
-                    kp_demig_tap(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
-                    kp_demig_tap(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
-                    kp_demig_tap(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
+                    const long long a1 = kp_f2ll_rn45(__fmul_rn(gs, fa));
+                    const long long b1 = kp_f2ll_rn45(__fmul_rn(gs, fb));
+                    const long long c1 = kp_f2ll_rn45(__fmul_rn(-2.0f * gs, f0));
+                    kp_demig_tap<SH>(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
+                    kp_demig_tap<SH>(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
+                    kp_demig_tap<SH>(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
                 }
             }
         }
     }
     /* order the row's atomics before the warp reads it back (past L1) */
-    __threadfence();
+    if (!SH) __threadfence();
     __syncwarp();
-    /* d = two reverse prefix sums of G, in place in the row (L2), lane l owning
+    /* the row's entries: shared memory (SH), or L2 past L1 */
+    auto ldg = [&](int i) -> unsigned long long {
+        if constexpr (SH) return Gg[i];
+        else return __ldcg(&Gg[i]);
+    };
+    auto stg = [&](int i, unsigned long long v) {
+        if constexpr (SH) Gg[i] = v;
+        else __stcg(&Gg[i], v);
+    };
+    /* d = two reverse prefix sums of G, in place in the row, lane l owning
        entries [l C, l C + C) */
     const int C = (ng + 31) >> 5;
     const int lo = min(ng, lane * C), hi = min(ng, lo + C);
     for (int pass = 0; pass < 2; ++pass) {
         unsigned long long tot = 0ull;
-        for (int i = lo; i < hi; ++i) tot += __ldcg(&Gg[i]);
+        for (int i = lo; i < hi; ++i) tot += ldg(i);
         unsigned long long incl = tot; /* sum over lanes >= lane */
         for (int d = 1; d < 32; d <<= 1) {
             const unsigned long long v = __shfl_down_sync(0xffffffffu, incl, d);
@@ -1039,19 +1100,19 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, 8) k_demig(KpDemigArgs a)
         }
         unsigned long long run = incl - tot;
         for (int i = hi - 1; i >= lo; --i) {
-            run += __ldcg(&Gg[i]);
-            __stcg(&Gg[i], run);
+            run += ldg(i);
+            stg(i, run);
         }
     }
     __syncwarp(); /* the lanes' rows are visible to the whole warp */
     float dmax = 0.0f;
     if (bound) {
-        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)__ldcg(&Gg[k])) * inv));
+        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)ldg(k)) * inv));
         dmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dmax)));
         if (lane == 0) a.dbound_out[slot] = dmax;
     } else {
         float *o = a.out + (int64_t)g.src * ns;
-        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)__ldcg(&Gg[k])), inv);
+        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)ldg(k)), inv);
     }
 }
 
