@@ -515,7 +515,7 @@ def run_lsm(args):
         torch.cuda.synchronize()
         secs = e0.elapsed_time(e1) / 1e3
         line["cg"] = {"iterations": args.cg_iters, "seconds": round(secs, 3),
-                      "applications": 2 * args.cg_iters + 1,
+                      "applications": 2 * args.cg_iters,
                       "residual_rel": [round(float(r / resid[0]), 6) for r in resid]}
     if args.lsm_accuracy > 0:
         line["lsm_accuracy"] = _lsm_accuracy(args, mdl, m, stream, dev)

@@ -270,7 +270,8 @@ int kpstm_lsm_adjoint(kpstm_ctx *ctx, const float *d_data, float *d_model);
    cull get zeros). */
 int kpstm_lsm_forward(kpstm_ctx *ctx, const float *d_model, float *d_data);
 /* Conjugate gradients on min ||L m - d||^2 (CGLS) from m = 0, niter
-   iterations, dot products and step lengths in FP64.  With
+   iterations (niter applications of L and of L^T: the last iteration skips
+   the next search direction), dot products and step lengths in FP64.  With
    KPSTM_PREC_BF16_KAHAN the data-domain vectors (d, residual) are stored
    as bf16 with a per-trace scale.  resid (nullable, niter + 1 values)
    receives ||d - L m_k||. */

@@ -1783,6 +1783,10 @@ extern "C" int kpstm_lsm_cg(kpstm_ctx *c, const float *d_data, int32_t niter, fl
                 if ((st = dot(c, r, r, nd, &rr))) break;
                 resid[it + 1] = sqrt(rr);
             }
+            if (it + 1 == niter) { /* x and r are final; the next direction (one L^T) is never used */
+                if (cudaGetLastError() != cudaSuccess) st = KPSTM_ERR_CUDA;
+                break;
+            }
             if ((st = adjoint_r(sv))) break;
             double gnew = 0.0;
             if ((st = dot(c, sv, sv, nm, &gnew))) break;
