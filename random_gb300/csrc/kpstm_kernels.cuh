@@ -835,7 +835,7 @@ struct KpDemigArgs {
     const int32_t *order;          /* [nlive] visiting order of the live slots, or null */
     float *dbound_out;             /* bound pass: receives dbound */
     float *out;                    /* [ntr][ns] in block order */
-    unsigned long long *acc;       /* [nlive][ng] zeroed fixed-point accumulators (L2-resident rows) */
+    unsigned long long *acc;       /* [nlive][ng] zeroed fixed-point rows in L2 (k_demig<false>); null when the rows are in shared memory */
     int *status;
     int nx, ny, ncls, ns, ng;      /* ng: accumulator entries per trace, ns + tm - 1 */
     int shift;                     /* bound pass: extra halvings of its scale (large images) */
