@@ -119,6 +119,103 @@ def algorithmic_bytes_per_step(model, ntr_step: int, row_floats: int) -> int:
     return ntr_step * row_floats * 4 + ntr_step * 32 + ncol * NS * 4 * 2 * 2 + NX * NS * 8
 
 
+
+# ------------------------------------------------------------------ roofline
+# Algorithmic operations of one pair (one pass of Kirchhoff.c:1374-1399),
+# counted as FP32-pipe lane operations (an FMA, an add, a compare, a shared
+# load each count 1) and MUFU operations:
+#   reference mode: 2 FMA for the two DSR arguments, 2 square roots, 1 add,
+#   1 multiply by 1/dt, 1 floor, 3 tap loads, 3 tap adds, 1 accumulate,
+#   1 fold increment, 1 compare = 14 FP32 + 2 MUFU;
+#   full mode adds ~4 FMA (interpolation, weights) and 1 MUFU (1/Lf).
+OPS_PER_PAIR = {"reference": (14, 2), "full": (18, 3), "full_bf16": (18, 3)}
+# which committed ncu summary holds the figures of each kernel flavour
+PROFILE_OF = {"full": "k_image_full_3d_ncu.md", "full_bf16": "k_image_full_3d_ncu.md",
+              "reference": "k_image_line_ncu.md"}
+KERNEL_SOURCES = ["random_gb300/csrc/kpstm_kernels.cuh", "random_gb300/csrc/kpstm_device.cuh"]
+
+
+def kernel_source_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update((ROOT / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profile_constants(name: str) -> dict | None:
+    """The machine-readable block of a committed ncu summary: the JSON code
+    block under its 'Bench constants' heading (figures of one capture, the
+    launch it was taken on and the kernel-source hash at capture time)."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    text = p.read_text()
+    i = text.find("## Bench constants")
+    if i < 0:
+        return None
+    j = text.find("```json", i)
+    k = text.find("```", j + 7)
+    if j < 0 or k < 0:
+        return None
+    return json.loads(text[j + 7:k])
+
+
+def imaging_roofline(pairs_per_launch, t_launch, b_alg, clk, peaks, dev, launch_cfg, flavour,
+                     table_rows=None, row_bytes=None) -> dict:
+    """Roofline of one imaging launch.  The binding resource is the FP32
+    lane-issue rate for the algorithmic op count (no tensor work; the kernel
+    moves ~1e-3 byte per pair): achieved = ops/pair x pairs/s, peak = SMs x
+    128 FP32 lanes x the SM clock sampled during the timed region.  HBM,
+    MUFU, issue slots and L2 are sub-fields; the ncu-derived figures come
+    from the committed summary of the same kernel flavour and are flagged
+    stale when the kernel sources or the launch differ from the capture."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clk.get("sm_mhz") or peaks["sm_max_mhz"]
+    rate = pairs_per_launch / t_launch
+    f32, mufu = OPS_PER_PAIR[flavour]
+    peak_ops = sms * 128 * mhz * 1e6
+    achieved = f32 * rate
+    out = {"bound": "fp32 lane issue (algorithmic ops)", "achieved": round(achieved / 1e12, 3),
+           "peak": round(peak_ops / 1e12, 3), "unit": "TFLOP/s", "frac": round(achieved / peak_ops, 4),
+           "ops_per_pair": {"fp32": f32, "mufu": mufu, "note": "lane operations; an FMA counts 1"},
+           "peak_basis": f"{sms} SMs x 128 FP32 lanes x {mhz:.0f} MHz (sampled)",
+           "launch_ms": round(t_launch * 1e3, 3), "pairs_per_launch": pairs_per_launch,
+           "hbm": {"achieved": round(b_alg / t_launch / 1e9, 3), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                   "frac": round(b_alg / t_launch / 1e9 / peaks["hbm_gbs"], 6), "peak_source": peaks["source"],
+                   "algorithmic_bytes_per_launch": b_alg},
+           "traffic": None}
+    pc = profile_constants(PROFILE_OF[flavour])
+    if pc is None:
+        out["profile"] = None
+        return out
+    cur = kernel_source_hash()
+    same_launch = all(pc.get("launch", {}).get(k) == launch_cfg.get(k)
+                      for k in ("tile_px", "samples_per_lane", "persistent", "ctas_per_sm"))
+    ipp = pc["warp_instructions"] / pc["pairs"]
+    issue_peak = sms * 4 * mhz * 1e6
+    out["issue_slots"] = {"instr_per_32_pairs": round(32 * ipp, 2),
+                          "frac": round(rate * ipp / issue_peak, 4),
+                          "ncu_issue_active": pc.get("issue_active")}
+    out["mufu"] = {"ops_per_pair": mufu, "ncu_xu_pipe": pc.get("xu_pipe")}
+    if pc.get("lts_bytes") is not None:
+        out["l2"] = {"achieved": round(pc["lts_bytes"] / pc["pairs"] * rate / 1e9, 1), "unit": "GB/s",
+                     "bytes_per_pair": round(pc["lts_bytes"] / pc["pairs"], 5),
+                     "ncu_lts_throughput": pc.get("lts_throughput")}
+    if pc.get("dram_bytes") is not None:
+        # fixed part (accumulators, velocity) + table part growing with the rows staged
+        extra = 0
+        if table_rows and pc.get("table_rows") and row_bytes:
+            extra = (table_rows - pc["table_rows"]) * row_bytes
+        out["traffic"] = round(pc["dram_bytes"] + extra)
+        out["traffic_source"] = (f"ncu dram bytes of the capture in profiles/{PROFILE_OF[flavour]} "
+                                 f"({pc.get('case', '')}), table part scaled to this launch")
+    out["profile"] = {"file": f"profiles/{PROFILE_OF[flavour]}", "kernel": pc.get("kernel"),
+                      "stale": pc.get("source_sha256") != cur or not same_launch,
+                      "source_sha256": cur, "captured_sha256": pc.get("source_sha256")}
+    return out
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_sample(n_traces: int, n_procs: int, opt: str = "-O3"):
     """The reference's kirchhoff() on this host's cores: the image is cut
@@ -248,32 +345,10 @@ def run_ours(args, rank, world, local_rank):
     row_floats = 2 * (NS + 2 * m.dims["trange_max"] - 2)
     row_floats = 8 + ((row_floats + 3) & ~3)  # geometry header + taps
     b_alg = algorithmic_bytes_per_step(model, block, row_floats)
-    achieved = b_alg / t_launch / 1e9
-    pairs_per_launch = pairs / launches
-    # DRAM traffic per launch from ncu (dram__bytes_read + write) of a
-    # 5,000-trace launch of the default kernel (3 CTAs/SM, K = 16, persistent)
-    # into the same image: 3.944e9 bytes, of which the tap tables are 5,000
-    # rows; the accumulator part is fixed, the table part grows with the traces
-    traffic = 3.944e9 + (block - 5000) * row_floats * 4
-    # issue-slot roofline: warp instructions per pair from a capture of the same
-    # launch (37.2 per 32 pairs) against 4 schedulers x SMs x the SM clock
-    instr_per_pair = 37.23 / 32
-    issue_peak = 4 * 152 * (clk.get("sm_mhz") or peaks["sm_max_mhz"]) * 1e6
-    issue_achieved = pairs_per_launch / t_launch * instr_per_pair
-    roofline = {
-        "bound": "hbm", "achieved": round(achieved, 3), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": round(achieved / peaks["hbm_gbs"], 6), "traffic": round(traffic),
-        "traffic_source": "ncu dram bytes of a 5,000-trace launch, table part scaled to the block",
-        "peak_source": peaks["source"], "kernel": "k_image (full mode)",
-        "algorithmic_bytes_per_launch": b_alg, "launch_ms": round(t_launch * 1e3, 3),
-        "pairs_per_launch": pairs_per_launch,
-        "binding": "SM instruction issue and latency (no tensor work; HBM bytes per pair are ~1e-3; "
-                   "FMA, ALU and SFU pipes each at most ~55% busy): see profiles/",
-        "issue": {"achieved": round(issue_achieved / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
-                  "unit": "T warp-instr/s", "frac": round(issue_achieved / issue_peak, 4),
-                  "instr_per_pair_source": "ncu smsp__inst_executed / pairs, 5,000-trace launch"},
-        "image_kernel_share": round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4),
-    }
+    roofline = imaging_roofline(pairs / launches, t_launch, b_alg, clk, peaks, dev, launch_cfg,
+                                "full_bf16" if args.precision == "bf16" else "full",
+                                table_rows=block, row_bytes=row_floats * 4)
+    roofline["image_kernel_share"] = round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4)
     del m
 
     # -------- e2e through the C ABI from pinned host memory
@@ -437,142 +512,275 @@ def run_line(args):
     print(json.dumps(line), flush=True)
 
 
-def run_lsm(args):
-    """Least-squares operator pair on 250,000 traces (ns = 751 at 4 ms,
-    offsets U(0, 3000 m), random azimuths) and a 200 x 200 x 751 model at
-    25 m, aperture 3000 m, full physics: a step is one demigration d = L m
-    plus one migration L^T d (the work of one CG iteration), BF16 data."""
+def lsm_problem(ntr: int, nx: int = 200, ny: int = 200, ns: int = 751, n_scat: int = 100, seed: int = 5):
+    """Config 5: the acquisition (synth.lsm_survey_model) and the seeded
+    reflectivity model m_true [nx, ny, 1, ns] (12 dipping reflectors and
+    n_scat scatterers); the data are d = L m_true plus 10 dB Gaussian noise,
+    made by the caller with its own L."""
+    from random_gb300 import synth
+    mdl = synth.lsm_survey_model(ntr, nx=nx, ny=ny, ns=ns, seed=seed)
+    p = mdl.survey.params
+    m_true = synth.reflectivity_model(nx, ny, ns, float(p["dt"]), 25.0, n_refl=12, n_scat=n_scat, seed=seed,
+                                      x0=p["start_iline"] * 25.0)
+    return mdl, m_true
+
+
+LSM_SNR_DB = 10.0
+
+
+def lsm_cpu_subproblem(args, dev, stream):
+    """The FP64-oracle leg of the least-squares workload (bench's CPU
+    baseline for it): a 16 x 16-column crop of config 5's model with 1,000
+    traces of the same acquisition statistics and 4 scatterers (the full
+    survey's scatterer density), d = L m_true (FP64 oracle) + 10 dB noise,
+    rounded to float32 for every solver.  The oracle's FP64 CGLS (timed on
+    the host cores) is the reference iterate for each k; the GPU's BF16- and
+    FP32-stored CGLS of the same data are compared with it at equal k."""
     import torch
-    from random_gb300 import build, capi, synth
+    from oracle import oracle
+    from random_gb300 import capi
+    from random_gb300.migration import Migration
+    mdl, m_true = lsm_problem(1000, nx=16, ny=16, n_scat=4, seed=7)
+    s = mdl.survey
+    d = oracle.lsm_apply(s, 1, m_true)
+    rng = np.random.default_rng(7)
+    d += rng.normal(0.0, float(np.sqrt(np.mean(d ** 2))) / 10.0 ** (LSM_SNR_DB / 20.0), d.shape)
+    d32 = d.astype(np.float32)
+    niter = args.cg_iters
+    t0 = time.perf_counter()
+    x64, res64 = oracle.cgls(s, d32.astype(np.float64), niter)
+    t_cpu = time.perf_counter() - t0
+    dd = torch.from_numpy(d32).to(dev)
+    out = {}
+    for name, prec in (("bf16", capi.PREC_BF16_KAHAN), ("fp32", capi.PREC_FP32)):
+        with Migration(dict(s.params, precision=prec), s.velocity) as mg:
+            mg.set_stream(stream.cuda_stream)
+            mg.lsm_geometry(s.headers)
+            xm = torch.empty(mg.shape, dtype=torch.float32, device=dev)
+            snaps = []
+            mg.lsm_cg(dd.data_ptr(), niter, xm.data_ptr(),
+                      monitor=lambda k, ptr, res: snaps.append(xm.to("cpu", copy=True).numpy()) and False)
+            out[name] = [float(np.linalg.norm(a.astype(np.float64).reshape(b.shape) - b) / np.linalg.norm(b))
+                         for a, b in zip(snaps, x64)]
+    pairs = 2 * niter * 1000 * 16 * 16 * 751  # upper bound: every (trace, column, sample) of the crop
+    return {"problem": "16 x 16 columns of config 5's model (25 m, 751 x 4 ms), 1,000 traces (offsets "
+                       "U(0, 3000 m), random azimuths, midpoints over the crop), 12 dipping reflectors + 4 "
+                       "scatterers, d = L m_true (FP64) + 10 dB noise, float32 data",
+            "rel_l2_vs_fp64": {k: [round(e, 8) for e in v] for k, v in out.items()},
+            "fp64_residual_rel": [round(float(r / res64[0]), 6) for r in res64],
+            "fp64_cgls_seconds": round(t_cpu, 2), "cores": host_cores(),
+            "fp64_pairs_bound": pairs}
+
+
+def run_lsm(args):
+    """Least-squares Kirchhoff migration, config 5: a 200 x 200 x 751
+    reflectivity model (25 m, 4 ms; 12 dipping reflectors + 100 scatterers),
+    d = L m_true on 250,000 traces (offsets U(0, 3000 m), random azimuths,
+    751 samples) plus 10 dB Gaussian noise, aperture 3000 m, full physics;
+    --cg-iters (20) CG iterations in BF16-stored / FP32-accumulated form with
+    FP64 scalars.  Reports the operator rates (L, L^T), the dot-product test
+    and --fd-dirs finite-difference checks at this size, the CG wall time and
+    residual history, one plain FP32 migration of the same survey, the
+    BF16 iterate's error against FP32-stored CGLS at full size
+    (--lsm-ref-iters iterations) and against the FP64 oracle's CGLS on a
+    sub-problem, and from these the wall time at which BF16 LSM first stays
+    within 1e-3 of the FP64-oracle iterate, in plain migrations."""
+    import torch
+    from random_gb300 import build, capi, segy
     from random_gb300.migration import Migration
     build.build()
     dev = torch.device("cuda", 0)
     ntr = args.survey_traces if args.survey_traces != SURVEY_TRACES else 250_000
-    mdl = synth.patch3d_model(ntr, ns=751, dt=0.004, nx=200, ny=200, bin_m=25.0, max_offset=3000.0, n_refl=12,
-                              n_diff=100, freq=25.0, aperture=3000.0, seed=5, mode=capi.MODE_FULL,
-                              output=capi.OUT_STACK)
+    mdl, m_true_np = lsm_problem(ntr)
     s = mdl.survey
-    m = Migration(dict(s.params, precision=capi.PREC_BF16_KAHAN), s.velocity)
+    ns = s.ns
     stream = torch.cuda.Stream(device=dev)
-    m.set_stream(stream.cuda_stream)
-    m.lsm_geometry(s.headers)
-    g = torch.Generator(device=dev)
-    g.manual_seed(5)
-    model = torch.randn(*m.shape, device=dev, generator=g)
-    data = torch.empty((ntr, 751), device=dev)
-    torch.cuda.synchronize()
-    t = {"fwd": 0.0, "adj": 0.0}
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-
-    def step(i):
-        ev[0].record(stream)
-        m.lsm_forward(model.data_ptr(), data.data_ptr())
-        ev[1].record(stream)
-        m.lsm_adjoint(data.data_ptr(), model.data_ptr())
-        ev[2].record(stream)
-        model.mul_(1.0 / (model.abs().max() + 1e-30))  # keep magnitudes bounded between steps
-        if i >= args.warmup:
-            torch.cuda.synchronize()
-            t["fwd"] += ev[0].elapsed_time(ev[1]) / 1e3
-            t["adj"] += ev[1].elapsed_time(ev[2]) / 1e3
-
-    with torch.cuda.stream(stream):
-        elapsed, clk = _timed_steps(step, args.warmup, args.steps, stream)
-    pairs_app = m.lsm_pairs()
-    line = {"workload": "lsm-operator-pair", "metric": METRIC,
-            "value": round(2 * pairs_app * args.steps / (t["fwd"] + t["adj"]) / 1e9, 4), "unit": UNIT,
-            "steps": args.steps, "warmup": args.warmup, "dtype": "bf16 data, f32 compute",
-            "forward_gpairs_s": round(pairs_app * args.steps / t["fwd"] / 1e9, 4),
-            "adjoint_gpairs_s": round(pairs_app * args.steps / t["adj"] / 1e9, 4),
-            "pairs_per_application": pairs_app,
-            "config": {"traces": ntr, "ns": 751, "model": "200x200x751", "aperture_m": 3000.0},
-            "clocks": clk}
-    if args.dot_test:
-        # adjointness at this size: |<L m, d> - <m, L^T d>| for seeded random m, d
-        gg = torch.Generator(device=dev)
-        gg.manual_seed(11)
-        mv = torch.randn(*m.shape, device=dev, generator=gg)
-        dv = torch.randn((ntr, 751), device=dev, generator=gg)
-        Lm = torch.empty_like(dv)
-        Ltd = torch.empty_like(mv)
-        m.lsm_forward(mv.data_ptr(), Lm.data_ptr())
-        m.lsm_adjoint(dv.data_ptr(), Ltd.data_ptr())
-        torch.cuda.synchronize()
-        a_ = float((Lm.double() * dv.double()).sum())
-        b_ = float((mv.double() * Ltd.double()).sum())
-        line["dot_test"] = {"rel": abs(a_ - b_) / abs(a_),
-                            "rel_to_norms": abs(a_ - b_) / float(Lm.double().norm() * dv.double().norm())}
-    if args.cg_iters > 0:
-        # least-squares migration of the survey's own events (bf16 data vectors,
-        # FP64 CG scalars): time and residual history of --cg-iters iterations
-        from random_gb300 import synth as _s
-        d_obs = _s.synthesize_torch(mdl, device=dev)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        resid = m.lsm_cg(d_obs.data_ptr(), args.cg_iters, model.data_ptr())
-        e1.record(stream)
-        torch.cuda.synchronize()
-        secs = e0.elapsed_time(e1) / 1e3
-        line["cg"] = {"iterations": args.cg_iters, "seconds": round(secs, 3),
-                      "applications": 2 * args.cg_iters,
-                      "residual_rel": [round(float(r / resid[0]), 6) for r in resid]}
-    if args.lsm_accuracy > 0:
-        line["lsm_accuracy"] = _lsm_accuracy(args, mdl, m, stream, dev)
-    print(json.dumps(line), flush=True)
-
-
-def _lsm_accuracy(args, mdl, m16, stream, dev):
-    """BF16-stored least-squares migration against FP32-stored CGLS of the
-    same data (FP64 dot products and step lengths in both; the FP32 solver
-    matches the FP64 oracle's CGLS to ~1e-6 relative where the oracle runs),
-    and the wall time of each against one plain FP32 migration of the same
-    survey (full mode: ingest, tap tables, imaging, finishing).  CGLS starts
-    from m = 0, so the iterate after k iterations comes from a k-iteration
-    run: each k is timed on its own."""
-    import numpy as np
-    import torch
-    from random_gb300 import capi, segy, synth
-    from random_gb300.migration import Migration
-    s = mdl.survey
-    d_obs = synth.synthesize_torch(mdl, device=dev)
-    m32 = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
-    m32.set_stream(stream.cuda_stream)
-    m32.lsm_geometry(s.headers)
-    x16 = torch.empty(*m16.shape, device=dev)
-    x32 = torch.empty_like(x16)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def timed(fn):
-        e0.record(stream)
+        a, b = ev(), ev()
+        a.record(stream)
         fn()
-        e1.record(stream)
+        b.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1e3
+        return a.elapsed_time(b) / 1e3
 
-    # plain FP32 migration of the same traces (second of two runs)
-    mp = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
-    mp.set_stream(stream.cuda_stream)
+    m16 = Migration(dict(s.params, precision=capi.PREC_BF16_KAHAN), s.velocity)
+    m16.set_stream(stream.cuda_stream)
+    m16.lsm_geometry(s.headers)
+    m_true = torch.from_numpy(m_true_np).to(dev)
+    d_obs = torch.empty((ntr, ns), device=dev)
+    model = torch.empty_like(m_true)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        # d = L m_true + 10 dB Gaussian noise (seeded)
+        m16.lsm_forward(m_true.data_ptr(), d_obs.data_ptr())
+        m16.lsm_adjoint(d_obs.data_ptr(), model.data_ptr())  # counts the pairs
+        torch.cuda.synchronize()
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(5)
+        sigma = float(d_obs.double().pow(2).mean().sqrt()) / 10.0 ** (LSM_SNR_DB / 20.0)
+        d_obs.add_(torch.randn(d_obs.shape, device=dev, generator=gen), alpha=sigma)
+        torch.cuda.synchronize()
+    pairs_app = m16.lsm_pairs()
+
+    # operator rates: --steps (L, L^T) applications after --warmup
+    tf, ta = [], []
+    d_tmp = torch.empty_like(d_obs)
+    clocks = None
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            clocks = ClockSampler(0)
+            clocks.start()
+        f = timed(lambda: m16.lsm_forward(m_true.data_ptr(), d_tmp.data_ptr()))
+        a = timed(lambda: m16.lsm_adjoint(d_obs.data_ptr(), model.data_ptr()))
+        if i >= args.warmup:
+            tf.append(f)
+            ta.append(a)
+    clk = clocks.stop() if clocks else None
+    t_L, t_Lt = statistics.median(tf), statistics.median(ta)
+    line = {"workload": "lsm",
+            "metric": "BF16 LSM wall time to 1e-3 FP64-oracle image error, in plain FP32 migrations of the survey",
+            "unit": "migrations", "higher_is_better": False,
+            "dtype": "bf16 data/residual store, f32 compute, f64 CG scalars",
+            "data": "synthetic: d = L m_true + 10 dB Gaussian noise (seeded)",
+            "config": {"workload": "config 5: 200x200x751 reflectivity (25 m, 4 ms), 12 dipping reflectors + 100 "
+                                   "scatterers, 250,000 traces x 751 samples, offsets U(0, 3000 m), random "
+                                   "azimuths, aperture 3000 m, full physics", "traces": ntr,
+                       "cg_iterations": args.cg_iters},
+            "pairs_per_application": pairs_app,
+            "operators": {"L_seconds": round(t_L, 4), "Lt_seconds": round(t_Lt, 4),
+                          "L_gpairs_s": round(pairs_app / t_L / 1e9, 2),
+                          "Lt_gpairs_s": round(pairs_app / t_Lt / 1e9, 2), "samples": len(tf)},
+            "clocks": clk}
+
+    # dot-product test at full size: <L m, d> = <m, L^T d> for seeded random m, d
+    gg = torch.Generator(device=dev)
+    gg.manual_seed(11)
+    mv = torch.randn(m_true.shape, device=dev, generator=gg)
+    dv = torch.randn((ntr, ns), device=dev, generator=gg)
+    Lm, Ltd = torch.empty_like(dv), torch.empty_like(mv)
+    with torch.cuda.stream(stream):
+        m16.lsm_forward(mv.data_ptr(), Lm.data_ptr())
+        m16.lsm_adjoint(dv.data_ptr(), Ltd.data_ptr())
+    torch.cuda.synchronize()
+    a_, b_ = float((Lm.double() * dv.double()).sum()), float((mv.double() * Ltd.double()).sum())
+    line["dot_test"] = {"rel": abs(a_ - b_) / abs(a_), "bar": 1e-5,
+                        "rel_to_norms": abs(a_ - b_) / float(Lm.double().norm() * dv.double().norm())}
+    del dv, Ltd
+
+    # finite-difference checks of the misfit gradient, J(m) = |L m - d|^2 / 2,
+    # g = L^T (L m - d), central differences along --fd-dirs random directions
+    if args.fd_dirs > 0:
+        with torch.cuda.stream(stream):
+            m16.lsm_forward(mv.data_ptr(), Lm.data_ptr())
+            res = Lm - d_obs
+            g = torch.empty_like(mv)
+            m16.lsm_adjoint(res.data_ptr(), g.data_ptr())
+            torch.cuda.synchronize()
+            worst, rels = 0.0, []
+            dm = torch.empty_like(mv)
+            mp = torch.empty_like(mv)
+            Lp = torch.empty_like(Lm)
+
+            def J(x):
+                m16.lsm_forward(x.data_ptr(), Lp.data_ptr())
+                torch.cuda.synchronize()
+                return 0.5 * float((Lp.double() - d_obs.double()).pow(2).sum())
+            for k in range(args.fd_dirs):
+                dm.normal_(generator=gg)
+                h = 1e-2 * float(mv.norm()) / float(dm.norm())
+                torch.add(mv, dm, alpha=h, out=mp)
+                jp = J(mp)
+                torch.add(mv, dm, alpha=-h, out=mp)
+                jm = J(mp)
+                fd = (jp - jm) / (2 * h)
+                an = float((g.double() * dm.double()).sum())
+                rels.append(abs(fd - an) / abs(an))
+            line["fd_check"] = {"directions": args.fd_dirs, "max_rel": max(rels),
+                                "median_rel": statistics.median(rels), "bar": 2e-3}
+            del res, g, dm, mp, Lp
+    del mv, Lm
+    torch.cuda.empty_cache()
+
+    # one plain FP32 migration of the same survey: ingest, tap tables, imaging, finishing
+    mp_ = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
+    mp_.set_stream(stream.cuda_stream)
     hdr_be = torch.from_numpy(np.ascontiguousarray(segy.headers_be(s.headers), dtype=np.int32)).to(dev)
-    img = torch.empty(*mp.shape, device=dev)
-    t_plain = 0.0
-    for _ in range(2):
-        mp.reset()
-        t_plain = timed(lambda: (mp.add_traces_device(hdr_be.data_ptr(), d_obs.data_ptr(), s.ntr),
-                                 mp.finish_device(img.data_ptr())))
-    err, t16, t32 = [], [], []
-    for k in range(1, args.lsm_accuracy + 1):
-        t16.append(timed(lambda: m16.lsm_cg(d_obs.data_ptr(), k, x16.data_ptr())))
-        t32.append(timed(lambda: m32.lsm_cg(d_obs.data_ptr(), k, x32.data_ptr())))
-        err.append(float((x16.double() - x32.double()).norm() / x32.double().norm()))
-    hit = next((k + 1 for k, e in enumerate(err) if e <= 1e-3), None)
-    return {"reference": "FP32-stored CGLS, FP64 scalars", "iterations": list(range(1, args.lsm_accuracy + 1)),
-            "rel_l2_bf16_vs_fp32": [round(e, 7) for e in err],
-            "bf16_seconds": [round(t, 3) for t in t16], "fp32_seconds": [round(t, 3) for t in t32],
-            "plain_fp32_migration_seconds": round(t_plain, 3),
-            "bf16_seconds_over_plain": [round(t / t_plain, 3) for t in t16],
-            "last_iteration_within_1e-3": max([k + 1 for k, e in enumerate(err) if e <= 1e-3], default=None),
-            "first_iteration_within_1e-3": hit}
+    img = torch.empty(mp_.shape, device=dev)
+    t_plain = []
+    for _ in range(3):
+        mp_.reset()
+        t_plain.append(timed(lambda: (mp_.add_traces_device(hdr_be.data_ptr(), d_obs.data_ptr(), ntr),
+                                      mp_.finish_device(img.data_ptr()))))
+    t_plain = min(t_plain[1:])
+    mp_.close()
+    del img, hdr_be
+    line["plain_fp32_migration_seconds"] = round(t_plain, 4)
+
+    # CGLS: BF16-stored (timed, with the iterate after every iteration) and
+    # FP32-stored (the full-size reference of the BF16 iterates)
+    def solve(mg, niter, keep):
+        snaps, marks = [], []
+        e0 = ev()
+
+        def mon(k, ptr, res):
+            e = ev()
+            e.record(stream)
+            marks.append(e)
+            if keep:
+                with torch.cuda.stream(stream):
+                    snaps.append(model.clone())
+            return False
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            resid = mg.lsm_cg(d_obs.data_ptr(), niter, model.data_ptr(), monitor=mon)
+        torch.cuda.synchronize()
+        return snaps, [e0.elapsed_time(e) / 1e3 for e in marks], resid
+
+    refk = min(args.lsm_ref_iters, args.cg_iters)
+    snaps16, tk, resid = solve(m16, args.cg_iters, refk > 0)
+    line["cg"] = {"iterations": len(tk), "seconds": round(tk[-1], 3) if tk else 0.0,
+                  "seconds_at_iteration": [round(t, 3) for t in tk],
+                  "seconds_over_plain_at_iteration": [round(t / t_plain, 3) for t in tk],
+                  "residual_rel": [round(float(r / resid[0]), 6) for r in resid],
+                  "applications": 2 * len(tk)}
+    m16.close()
+    err_full = []
+    if refk > 0:
+        m32 = Migration(dict(s.params, precision=capi.PREC_FP32), s.velocity)
+        m32.set_stream(stream.cuda_stream)
+        m32.lsm_geometry(s.headers)
+        snaps32, _, _ = solve(m32, refk, True)
+        m32.close()
+        err_full = [float((a.double() - b.double()).norm() / b.double().norm()) for a, b in zip(snaps16, snaps32)]
+        line["bf16_vs_fp32_full_size"] = [round(e, 8) for e in err_full]
+    del snaps16
+    torch.cuda.empty_cache()
+
+    sub = None
+    if not args.no_cpu:
+        sub = lsm_cpu_subproblem(args, dev, stream)
+        line["fp64_subproblem"] = sub
+        line["cpu_baseline"] = {"value": sub["fp64_cgls_seconds"], "unit": "s (FP64 oracle CGLS, sub-problem)",
+                                "cores": sub["cores"], "kind": "port",
+                                "sample": f"{args.cg_iters} CG iterations of the FP64 oracle on the 16 x 16-column, "
+                                          f"1,000-trace sub-problem"}
+    # BF16 iterate k is within 1e-3 of the FP64-oracle iterate when the full-size
+    # BF16-vs-FP32 error plus the sub-problem's FP32-vs-FP64 gap is at most 1e-3
+    # and the sub-problem's BF16-vs-FP64 error is too
+    within = []
+    for k in range(len(tk)):
+        e = err_full[k] if k < len(err_full) else None
+        gap = sub["rel_l2_vs_fp64"]["fp32"][k] if sub and k < len(sub["rel_l2_vs_fp64"]["fp32"]) else 0.0
+        eb = sub["rel_l2_vs_fp64"]["bf16"][k] if sub and k < len(sub["rel_l2_vs_fp64"]["bf16"]) else 0.0
+        within.append(e is not None and e + gap <= 1e-3 and eb <= 1e-3)
+    kstar = next((k for k in range(len(within)) if all(within[k:])), None)
+    line["within_1e-3_at_iteration"] = within
+    line["value"] = round(tk[kstar] / t_plain, 4) if kstar is not None else None
+    line["first_iteration_staying_within_1e-3"] = None if kstar is None else kstar + 1
+    line["target"] = "< 10 plain FP32 migrations"
+    print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------- reference arm
@@ -616,11 +824,11 @@ def main():
     ap.add_argument("--ref-traces", type=int, default=1500)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cg-iters", type=int, default=0, help="lsm workload: also time this many CG iterations")
-    ap.add_argument("--dot-test", action="store_true", help="lsm workload: also run the dot-product test")
-    ap.add_argument("--lsm-accuracy", type=int, default=0,
-                    help="lsm workload: BF16 vs FP32 CGLS iterates and times for 1..N iterations, "
-                         "against one plain FP32 migration of the same survey")
+    ap.add_argument("--cg-iters", type=int, default=20, help="lsm workload: CG iterations")
+    ap.add_argument("--lsm-ref-iters", type=int, default=20,
+                    help="lsm workload: iterations of the full-size FP32-stored reference CGLS (0: none)")
+    ap.add_argument("--fd-dirs", type=int, default=16,
+                    help="lsm workload: finite-difference checks of the misfit gradient (random directions)")
     ap.add_argument("--autotune", type=int, default=0,
                     help="survey workload: autotune the launch on this many traces before timing (0: default launch)")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",

@@ -276,6 +276,16 @@ int kpstm_lsm_forward(kpstm_ctx *ctx, const float *d_model, float *d_data);
    as bf16 with a per-trace scale.  resid (nullable, niter + 1 values)
    receives ||d - L m_k||. */
 int kpstm_lsm_cg(kpstm_ctx *ctx, const float *d_data, int32_t niter, float *d_model, double *resid);
+/* Called by kpstm_lsm_cg_ex after iteration k (1 .. niter) has updated the
+   model: d_model (device memory) holds the iterate m_k and resid_k =
+   ||d - L m_k||.  Device work the monitor queues on the context's stream
+   (kpstm_set_stream) sees m_k; the next iteration starts after the monitor
+   returns.  A nonzero return ends the solve after this iteration. */
+typedef int (*kpstm_cg_monitor)(int32_t iteration, const float *d_model, double resid_k, void *user);
+/* kpstm_lsm_cg with a monitor (nullable): snapshots, wall-clock marks or a
+   stopping rule per iteration. */
+int kpstm_lsm_cg_ex(kpstm_ctx *ctx, const float *d_data, int32_t niter, float *d_model, double *resid,
+                    kpstm_cg_monitor monitor, void *user);
 /* Pairs (trace, in-aperture column, sample) of one operator application,
    counted by the last kpstm_lsm_adjoint (L visits the same pairs). */
 int kpstm_lsm_pair_count(kpstm_ctx *ctx, int64_t *pairs);

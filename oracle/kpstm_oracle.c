@@ -470,7 +470,116 @@ done:
 /* Least-squares operator pair (full physics, see full_pairs), in double.
    The pair set and the geometry follow ko_kirchhoff exactly; every pair
    couples data sample k of the trace with model sample t of the column by
-   t0 (1/ts + 1/tr)^2 / (8 Lf^2) * max(0, Lf - |T - k|). */
+   t0 (1/ts + 1/tr)^2 / (8 Lf^2) * max(0, Lf - |T - k|).
+   Threads: L^T (direction 0) splits the image columns, L (direction 1) the
+   traces, so every output element is summed by one thread in the order of
+   the single-threaded loop (traces in order for a model sample, columns in
+   (xc, yc) order for a data sample) and the result does not depend on the
+   thread count. */
+typedef struct {
+    float sxt, syt, gxt, gyt, cmpx, cmpy;
+    int off, live;
+} ko_lgeom;
+
+typedef struct {
+    const kpstm_params *p;
+    const ko_dims *d;
+    const ko_lgeom *geom;
+    const double *vcol;    /* [ncol][ns] v_rms per column and sample, or NaN row: below the grid */
+    int64_t ntr;
+    int direction, lmax;
+    const double *in;
+    double *out;
+    int64_t next;
+    int err;
+    pthread_mutex_t mu;
+} ko_ljob;
+
+/* the pairs of (trace g, column col): d = L m adds to out_d, m = L^T d adds to out_m */
+static int ko_lsm_pairs(const ko_ljob *J, const ko_lgeom *g, int64_t it, int col)
+{
+    const kpstm_params *p = J->p;
+    const ko_dims *d = J->d;
+    const int ns = d->ns, nh = d->nh;
+    const int xc = col / d->ny, yc = col % d->ny;
+    float IX = (float)((p->start_iline + ((xc + d->xslice * d->nx) * p->inc_iline)) * p->iline_distance);
+    float IY = (float)((p->start_xline + ((yc + d->yslice * d->ny) * p->inc_xline)) * p->xline_distance);
+    float cdx = IX - g->cmpx, cdy = IY - g->cmpy;
+    float dC = sqrtf(cdx * cdx + cdy * cdy);
+    if (!((double)dC < p->aperture)) return 0;
+    const double *vcol = J->vcol + (size_t)col * ns;
+    if (vcol[0] != vcol[0]) return KPSTM_ERR_VELOCITY_RANGE;
+    const double dt = (double)p->dt;
+    const double ax = p->iline_distance / dt, ay = p->xline_distance / dt;
+    const double sx = (double)IX - g->sxt, sy = (double)IY - g->syt;
+    const double gx = (double)IX - g->gxt, gy = (double)IY - g->gyt;
+    const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
+    const size_t mbase = ((size_t)col * nh + g->off) * ns;
+    const size_t dbase = (size_t)it * ns;
+    for (int t = 1; t < ns; ++t) {
+        /* v^2 as the product stores it: the node's float square, or the
+           interpolated v_rms squared in double, rounded to float */
+        const float vvf = p->velocity_interp ? (float)(vcol[t] * vcol[t]) : (float)vcol[t] * (float)vcol[t];
+        double rv2 = 1.0 / (double)vvf;
+        double t0 = (double)t * dt;
+        double th2 = 0.25 * t0 * t0;
+        double ts = sqrt(th2 + dS2 * rv2), tr = sqrt(th2 + dR2 * rv2);
+        double T = (ts + tr) / dt;
+        if (!(T < ns - 1)) continue;
+        double Lf = 1.0 + fabs((sx / ts + gx / tr) * rv2 * ax) + fabs((sy / ts + gy / tr) * rv2 * ay);
+        if (Lf > J->lmax) Lf = J->lmax;
+        double u = 1.0 / ts + 1.0 / tr;
+        double W = t0 / 8.0 * u * u / (Lf * Lf);
+        int k0 = (int)ceil(T - Lf), k1 = (int)floor(T + Lf);
+        if (k0 < 0) k0 = 0;
+        if (k1 > ns - 1) k1 = ns - 1;
+        if (J->direction == 0) {
+            double tri = 0.0;
+            for (int k = k0; k <= k1; ++k) {
+                double wk = Lf - fabs(T - k);
+                if (wk > 0) tri += J->in[dbase + k] * wk;
+            }
+            J->out[mbase + t] += W * tri;
+        } else {
+            double mv = W * J->in[mbase + t];
+            for (int k = k0; k <= k1; ++k) {
+                double wk = Lf - fabs(T - k);
+                if (wk > 0) J->out[dbase + k] += mv * wk;
+            }
+        }
+    }
+    return 0;
+}
+
+static void *ko_lsm_worker(void *arg)
+{
+    ko_ljob *J = (ko_ljob *)arg;
+    const int ncol = J->d->nx * J->d->ny;
+    const int64_t nunit = J->direction == 0 ? ncol : J->ntr;
+    int st = 0;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        const int64_t u = J->next++;
+        const int stop = J->err != 0;
+        pthread_mutex_unlock(&J->mu);
+        if (u >= nunit || stop) break;
+        if (J->direction == 0) { /* one column, every trace in order */
+            for (int64_t it = 0; it < J->ntr && !st; ++it)
+                if (J->geom[it].live) st = ko_lsm_pairs(J, &J->geom[it], it, (int)u);
+        } else { /* one trace, every column in order */
+            if (J->geom[u].live)
+                for (int col = 0; col < ncol && !st; ++col) st = ko_lsm_pairs(J, &J->geom[u], u, col);
+        }
+        if (st) {
+            pthread_mutex_lock(&J->mu);
+            J->err = st;
+            pthread_mutex_unlock(&J->mu);
+            break;
+        }
+    }
+    return NULL;
+}
+
 int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *hdr_be, int64_t ntr,
                  int direction, const double *in, double *out)
 {
@@ -479,7 +588,7 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
     ko_dims d;
     int st = ko_dims_of(p, &d);
     if (st) return st;
-    const int ns = d.ns, nh = d.nh;
+    const int ns = d.ns, nh = d.nh, ncol = d.nx * d.ny;
     int tm;
     ko_aliasfilter(ns, p->dt, p->iline_distance, p->xline_distance, p->anti_alias_cutoff, &tm, NULL);
     if (tm < 2) return KPSTM_ERR_TRANGE;
@@ -487,100 +596,70 @@ int ko_lsm_apply(const kpstm_params *p, const kpstm_velocity *v, const int32_t *
     if (lmax > tm - 1) lmax = tm - 1;
     if (lmax > 63) lmax = 63;
     if (lmax < 1) lmax = 1;
-    const size_t nmod = (size_t)d.nx * d.ny * nh * ns;
+    const size_t nmod = (size_t)ncol * nh * ns;
     if (direction == 0) memset(out, 0, sizeof(double) * nmod);
     else memset(out, 0, sizeof(double) * (size_t)ntr * ns);
-    int *t1 = (int *)malloc(sizeof(int) * ns);
-    double *vcol = (double *)malloc(sizeof(double) * ns);
-    if (!t1 || !vcol) {
-        free(t1);
+    ko_lgeom *geom = (ko_lgeom *)malloc(sizeof(ko_lgeom) * (size_t)ntr);
+    double *vcol = (double *)malloc(sizeof(double) * (size_t)ncol * ns);
+    if (!geom || !vcol) {
+        free(geom);
         free(vcol);
         return KPSTM_ERR_OUT_OF_MEMORY;
     }
-    for (int t = 0; t < ns; ++t) {
-        int q = (int)round((double)((float)t * (p->dt / v->dtm)));
-        t1[t] = q > v->nsm - 1 ? v->nsm - 1 : q;
+    for (int col = 0; col < ncol; ++col) { /* v_rms of every column once (NaN row: below the grid) */
+        double *vc = vcol + (size_t)col * ns;
+        if (ko_col_vrms(p, v, col / d.ny + d.xslice * d.nx, col % d.ny + d.yslice * d.ny, ns, vc))
+            for (int t = 0; t < ns; ++t) vc[t] = NAN;
     }
     float IXc = (float)((p->start_iline + ((d.nx / 2.0 + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance);
     float IYc = (float)((p->start_xline + ((d.ny / 2.0 + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance);
     float add_on = (float)(0.5 * sqrt(d.nx * p->inc_iline * p->iline_distance * d.nx * p->inc_iline * p->iline_distance +
                                       d.ny * p->inc_xline * p->xline_distance * d.ny * p->inc_xline * p->xline_distance));
-    const double dt = (double)p->dt;
-    const double ax = p->iline_distance / dt, ay = p->xline_distance / dt;
-    for (int64_t it = 0; it < ntr && !st; ++it) {
+    for (int64_t it = 0; it < ntr; ++it) { /* geometry, class and slab cull as ko_kirchhoff */
         const int32_t *h = hdr_be + (size_t)it * 60;
         double w4[4];
         for (int k = 0; k < 4; ++k) w4[k] = (double)be32(h[18 + k]) - (k % 2 == 0 ? p->ox : p->oy);
-        ko_geom g;
+        ko_lgeom *g = &geom[it];
         int i = (int)w4[0], j = (int)w4[1];
-        g.sxt = d.cosA * (float)i + d.sinA * (float)j;
-        g.syt = -d.sinA * (float)i + d.cosA * (float)j;
+        g->sxt = d.cosA * (float)i + d.sinA * (float)j;
+        g->syt = -d.sinA * (float)i + d.cosA * (float)j;
         i = (int)w4[2];
         j = (int)w4[3];
-        g.gxt = d.cosA * (float)i + d.sinA * (float)j;
-        g.gyt = -d.sinA * (float)i + d.cosA * (float)j;
-        float h2 = (float)(0.25 * (double)((g.sxt - g.gxt) * (g.sxt - g.gxt) + (g.syt - g.gyt) * (g.syt - g.gyt)));
-        g.cmpx = (float)(0.5 * (double)(g.sxt + g.gxt));
-        g.cmpy = (float)(0.5 * (double)(g.syt + g.gyt));
+        g->gxt = d.cosA * (float)i + d.sinA * (float)j;
+        g->gyt = -d.sinA * (float)i + d.cosA * (float)j;
+        float h2 = (float)(0.25 * (double)((g->sxt - g->gxt) * (g->sxt - g->gxt) + (g->syt - g->gyt) * (g->syt - g->gyt)));
+        g->cmpx = (float)(0.5 * (double)(g->sxt + g->gxt));
+        g->cmpy = (float)(0.5 * (double)(g->syt + g->gyt));
         int off = (int)floor((2.0 * sqrt((double)h2) - p->oh) / p->dh);
-        if (!(off >= 0 && off < p->nh)) continue;
-        if (p->output == KPSTM_OUT_STACK) off = 0;
-        float dIC = sqrtf((IXc - g.cmpx) * (IXc - g.cmpx) + (IYc - g.cmpy) * (IYc - g.cmpy));
-        if (!((double)dIC < p->aperture + (double)add_on)) continue;
-        for (int xc = 0; xc < d.nx; ++xc) {
-            for (int yc = 0; yc < d.ny; ++yc) {
-                float IX = (float)((p->start_iline + ((xc + d.xslice * d.nx) * p->inc_iline)) * p->iline_distance);
-                float IY = (float)((p->start_xline + ((yc + d.yslice * d.ny) * p->inc_xline)) * p->xline_distance);
-                float cdx = IX - g.cmpx, cdy = IY - g.cmpy;
-                float dC = sqrtf(cdx * cdx + cdy * cdy);
-                if (!((double)dC < p->aperture)) continue;
-                if (ko_col_vrms(p, v, xc + d.xslice * d.nx, yc + d.yslice * d.ny, ns, vcol)) {
-                    st = KPSTM_ERR_VELOCITY_RANGE;
-                    break;
-                }
-                const double sx = (double)IX - g.sxt, sy = (double)IY - g.syt;
-                const double gx = (double)IX - g.gxt, gy = (double)IY - g.gyt;
-                const double dS2 = sx * sx + sy * sy, dR2 = gx * gx + gy * gy;
-                const size_t mbase = (((size_t)xc * d.ny + yc) * nh + off) * ns;
-                const size_t dbase = (size_t)it * ns;
-                for (int t = 1; t < ns; ++t) {
-                    /* v^2 as the product stores it: the node's float square, or
-                       the interpolated v_rms squared in double, rounded to float */
-                    const float vvf = p->velocity_interp ? (float)(vcol[t] * vcol[t])
-                                                         : (float)vcol[t] * (float)vcol[t];
-                    double rv2 = 1.0 / (double)vvf;
-                    double t0 = (double)t * dt;
-                    double th2 = 0.25 * t0 * t0;
-                    double ts = sqrt(th2 + dS2 * rv2), tr = sqrt(th2 + dR2 * rv2);
-                    double T = (ts + tr) / dt;
-                    if (!(T < ns - 1)) continue;
-                    double Lf = 1.0 + fabs((sx / ts + gx / tr) * rv2 * ax) + fabs((sy / ts + gy / tr) * rv2 * ay);
-                    if (Lf > lmax) Lf = lmax;
-                    double u = 1.0 / ts + 1.0 / tr;
-                    double W = t0 / 8.0 * u * u / (Lf * Lf);
-                    int k0 = (int)ceil(T - Lf), k1 = (int)floor(T + Lf);
-                    if (k0 < 0) k0 = 0;
-                    if (k1 > ns - 1) k1 = ns - 1;
-                    if (direction == 0) {
-                        double tri = 0.0;
-                        for (int k = k0; k <= k1; ++k) {
-                            double wk = Lf - fabs(T - k);
-                            if (wk > 0) tri += in[dbase + k] * wk;
-                        }
-                        out[mbase + t] += W * tri;
-                    } else {
-                        double mv = W * in[mbase + t];
-                        for (int k = k0; k <= k1; ++k) {
-                            double wk = Lf - fabs(T - k);
-                            if (wk > 0) out[dbase + k] += mv * wk;
-                        }
-                    }
-                }
-            }
-            if (st) break;
-        }
+        g->live = off >= 0 && off < p->nh;
+        g->off = p->output == KPSTM_OUT_STACK ? 0 : off;
+        float dIC = sqrtf((IXc - g->cmpx) * (IXc - g->cmpx) + (IYc - g->cmpy) * (IYc - g->cmpy));
+        if (!((double)dIC < p->aperture + (double)add_on)) g->live = 0;
     }
-    free(t1);
+    ko_ljob J;
+    memset(&J, 0, sizeof(J));
+    J.p = p;
+    J.d = &d;
+    J.geom = geom;
+    J.vcol = vcol;
+    J.ntr = ntr;
+    J.direction = direction;
+    J.lmax = lmax;
+    J.in = in;
+    J.out = out;
+    pthread_mutex_init(&J.mu, NULL);
+    long ncpu = sysconf(_SC_NPROCESSORS_ONLN);
+    int nth = ncpu > 0 ? (int)ncpu : 1;
+    if (nth > 256) nth = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int k = 1; k < nth; ++k)
+        if (pthread_create(&th[started], NULL, ko_lsm_worker, &J) == 0) ++started;
+    ko_lsm_worker(&J);
+    for (int k = 0; k < started; ++k) pthread_join(th[k], NULL);
+    pthread_mutex_destroy(&J.mu);
+    st = J.err;
+    free(geom);
     free(vcol);
     return st;
 }

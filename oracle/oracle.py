@@ -145,3 +145,34 @@ def kirchhoff64(survey, params: dict | None = None):
     if st:
         raise RuntimeError(f"ko_kirchhoff64: status {st}")
     return out
+
+
+def cgls(survey, d: np.ndarray, niter: int, params: dict | None = None):
+    """FP64 CGLS on min |L m - d|^2 from m = 0 with the oracle operators
+    (lsm_apply), the same recurrence as the library's kpstm_lsm_cg: r = d,
+    s = L^T r, p = s; per iteration q = L p, alpha = |s|^2/|q|^2,
+    m += alpha p, r -= alpha q, s = L^T r, beta = |s_new|^2/|s|^2,
+    p = s + beta p (the last iteration stops after the update of m and r).
+    Returns (iterates [niter] of float64 models, residual norms [niter + 1])."""
+    d = np.asarray(d, np.float64)
+    r = d.copy()
+    s_ = lsm_apply(survey, 0, r, params)
+    p = s_.copy()
+    x = np.zeros_like(s_)
+    gamma = float(np.vdot(s_, s_))
+    res, xs = [float(np.linalg.norm(r))], []
+    for it in range(niter):
+        q = lsm_apply(survey, 1, p, params)
+        qq = float(np.vdot(q, q))
+        alpha = gamma / qq if qq > 0 else 0.0
+        x += alpha * p
+        r -= alpha * q
+        res.append(float(np.linalg.norm(r)))
+        xs.append(x.copy())
+        if it + 1 == niter:
+            break
+        s_ = lsm_apply(survey, 0, r, params)
+        gnew = float(np.vdot(s_, s_))
+        p = s_ + (gnew / gamma if gamma > 0 else 0.0) * p
+        gamma = gnew
+    return xs, np.array(res)

@@ -29,6 +29,9 @@ STATUS = {
 }
 NOALLOC_MAX_SAMPLES = 4194304
 
+# kpstm_cg_monitor: int (*)(int32_t iteration, const float *d_model, double resid_k, void *user)
+CG_MONITOR = C.CFUNCTYPE(C.c_int, C.c_int32, C.c_void_p, C.c_double, C.c_void_p)
+
 
 class KpstmParams(C.Structure):
     _fields_ = [
@@ -154,6 +157,7 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_lsm_adjoint", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_lsm_forward", C.c_int, [_VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_lsm_cg", C.c_int, [_VOIDP, _VOIDP, C.c_int32, _VOIDP, _VOIDP])
+    _sig(lib, "kpstm_lsm_cg_ex", C.c_int, [_VOIDP, _VOIDP, C.c_int32, _VOIDP, _VOIDP, CG_MONITOR, _VOIDP])
     _sig(lib, "kpstm_lsm_pair_count", C.c_int, [_VOIDP, C.POINTER(i64)])
     _sig(lib, "kpstm_finish_noalloc", C.c_int, [C.POINTER(KpstmParams), _VOIDP, _VOIDP, _VOIDP, _VOIDP])
     _sig(lib, "kpstm_aliasfilter", C.c_int, [i32, C.c_float, C.c_double, C.c_double, C.c_double,

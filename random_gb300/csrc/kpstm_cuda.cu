@@ -97,6 +97,7 @@ struct kpstm_ctx {
     double *d_dotpart, *d_dot;
     unsigned int *d_absmax;      /* demigration: bits of max |model| */
     float *d_dbound;             /* demigration: per live trace max_k (L 1)[k] */
+    float *d_wbound;             /* demigration: per live trace largest pair weight x t/(8 dt) */
     unsigned long long *d_dacc;  /* demigration: [nlive][ng] fixed-point trace accumulators */
     int32_t *d_dorder;           /* demigration: live slots in Morton order of their midpoints */
     float *d_rvdt;               /* demigration: [nrow][ns] 1/(v dt)^2 */
@@ -803,7 +804,7 @@ static int kp_free_all(kpstm_ctx *c)
                     c->d_smp[1], c->d_raw[0], c->d_raw[1], c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
                     c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive, c->d_lcnt, c->d_ltable, c->d_lkm,
                     c->d_lhits, c->d_dotpart, c->d_dot, c->d_smp16, c->d_scl16, c->d_tilecols, c->d_queue,
-                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder, c->d_rvdt};
+                    c->d_clsorder, c->d_absmax, c->d_dbound, c->d_wbound, c->d_lkc, c->d_dacc, c->d_dorder, c->d_rvdt};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i)
         if (ptrs[i]) cudaFree(ptrs[i]);
     for (int k = 0; k < 2; ++k) {
@@ -1457,15 +1458,40 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.aay = (float)p->xline_distance;
     a.dt = p->dt;
     a.ng = ns + s->dims.trange_max - 1; /* G index <= ns - 1 + lmax, lmax <= tm - 1 */
-    /* |d| 2^E < 2^63 needs (columns x samples x lmax) < 2^33 (worst case: every
-       pair of the trace covering one sample with weight bound and width lmax) */
-    const double cover = (double)s->ncol * ns * (s->lmax > 1 ? s->lmax : 1);
-    a.shift = cover > 8589934592.0 ? (int)ceil(log2(cover / 8589934592.0)) : 0;
+    /* Worst case of one trace: every (column, sample) pair of the slab covering
+       one sample with the largest weight and width lmax + 1 (the triangle plus
+       the float rounding of its tap positions). */
+    const double cover = (double)s->ncol * ns * (s->lmax + 1);
+    /* Below its support a pair leaves gs (ya + yb - 2 y0) in every sample, |.|
+       <= one spacing u of floats below 2^ceil(log2 ng) (the roundings of
+       y0 +- Lf).  Summed over a trace's pairs that is at most u max|m| sum(w ts),
+       and sum(w ts) <= 2 sum_k (L 1)[k] <= 2 ng (L 1)max (a triangle of
+       half-width Lf >= 1 sums to at least Lf^2 / 2 over the samples), so the
+       tails add at most 2 ng u = tailf times (L 1)max; twice that is used. */
+    {
+        const int eg = (int)ceil(log2((double)a.ng + 1.0));
+        a.tailf = (float)(4.0 * a.ng * ldexp(1.0, eg - 24));
+    }
+    /* shared-memory rows: an entry gets at most 4 units of 2^(R-1) per sample
+       of a column; norm_cols columns between normalisations must keep the low
+       limb within 2^31: (4 ns norm_cols + 2) 2^(R-1) <= 2^31 */
+    a.norm_cols = 2;
+    a.limb_r = 32 - (int)ceil(log2(4.0 * ns * a.norm_cols + 2.0));
+    while (a.limb_r < 12 && a.norm_cols > 1) {
+        a.norm_cols /= 2;
+        a.limb_r = 32 - (int)ceil(log2(4.0 * ns * a.norm_cols + 2.0));
+    }
+    if (a.limb_r > 21) a.limb_r = 21;
     a.absmax = c->d_absmax;
     a.order = c->d_dorder;
     /* accumulator rows in shared memory when four of them fit with room for
-       several CTAs per SM, else in L2 */
-    const bool use_sh = kp_demig_smem(ns, a.ng, true) <= 48 * 1024;
+       several CTAs per SM (and the radix leaves the limbs room), else in L2 */
+    const bool use_sh = kp_demig_smem(ns, a.ng, true) <= 48 * 1024 && a.limb_r >= 12;
+    /* bound pass (all-ones model, |gs| < 2^bound_g): shared rows need
+       4 cover 2^g + 2^31 < 2^(31+R) and |2 gs| < 2^(22+R); the L2 rows need
+       cover 2^g < 2^62 and |2 gs| <= 2^45 */
+    const int lc = (int)ceil(log2(cover));
+    a.bound_g = use_sh ? (21 < 28 - lc ? 21 : 28 - lc) + a.limb_r : (30 < 61 - lc ? 30 : 61 - lc);
     const size_t smem = kp_demig_smem(ns, a.ng, use_sh);
     if (smem > 200 * 1024) return KPSTM_ERR_UNSUPPORTED;
     const size_t accb = sizeof(unsigned long long) * (size_t)a.ng * (size_t)c->lsm_nlive;
@@ -1489,6 +1515,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
         KpDemigArgs b = a;
         b.model = nullptr;
         b.dbound_out = c->d_dbound;
+        b.wbound_out = c->d_wbound;
         if (!use_sh) KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
         dm<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
         KP_CUDA(cudaGetLastError());
@@ -1496,6 +1523,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     }
     if (!use_sh) KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
     a.dbound = c->d_dbound;
+    a.wbound = c->d_wbound;
     const int64_t nmodel = (int64_t)s->nclass * s->ncol * ns;
     KP_CUDA(cudaMemsetAsync(c->d_absmax, 0, sizeof(unsigned int), c->cs));
     k_absmax<<<4 * c->nsm, 256, 0, c->cs>>>(d_model, nmodel, c->d_absmax);
@@ -1596,7 +1624,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
     KP_CUDA(cudaStreamSynchronize(c->cs));
     void *old[] = {c->d_lgraw, c->d_lgeom, c->d_lcls, c->d_lorder, c->d_lcstart, c->d_lnlive,
                    c->d_lcnt, c->d_ltable, c->d_lkm, c->d_lhits, c->d_dotpart, c->d_dot, c->d_absmax,
-                   c->d_dbound, c->d_lkc, c->d_dacc, c->d_dorder};
+                   c->d_dbound, c->d_wbound, c->d_lkc, c->d_dacc, c->d_dorder};
     for (size_t i = 0; i < sizeof(old) / sizeof(old[0]); ++i)
         if (old[i]) cudaFree(old[i]);
     c->d_lkc = nullptr;
@@ -1604,6 +1632,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
     c->d_dorder = nullptr;
     c->d_absmax = nullptr;
     c->d_dbound = nullptr;
+    c->d_wbound = nullptr;
     c->dbound_ok = 0;
     c->d_lgraw = c->d_lgeom = nullptr;
     c->d_lcls = c->d_lorder = c->d_lcstart = c->d_lnlive = c->d_lcnt = nullptr;
@@ -1639,6 +1668,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         KP_LALLOC(c->d_dot, sizeof(double) * 4);
         KP_LALLOC(c->d_absmax, sizeof(unsigned int));
         KP_LALLOC(c->d_dbound, sizeof(float) * (size_t)ntr);
+        KP_LALLOC(c->d_wbound, sizeof(float) * (size_t)ntr);
         if (c->p.precision == KPSTM_PREC_BF16_KAHAN) KP_LALLOC(c->d_lkc, sizeof(float) * nimg);
 #undef KP_LALLOC
         if (cudaMemcpyAsync(d_hdr, hdr_be, sizeof(int32_t) * 60 * ntr, cudaMemcpyHostToDevice, c->cs) !=
@@ -1724,6 +1754,12 @@ static int dot(kpstm_ctx *c, const float *x, const float *y, int64_t n, double *
    x += alpha p, r -= alpha q, s = L^T r, beta = |s_new|^2/|s|^2, p = s + beta p. */
 extern "C" int kpstm_lsm_cg(kpstm_ctx *c, const float *d_data, int32_t niter, float *d_model, double *resid)
 {
+    return kpstm_lsm_cg_ex(c, d_data, niter, d_model, resid, nullptr, nullptr);
+}
+
+extern "C" int kpstm_lsm_cg_ex(kpstm_ctx *c, const float *d_data, int32_t niter, float *d_model, double *resid,
+                               kpstm_cg_monitor monitor, void *user)
+{
     if (!c || !d_data || !d_model || niter < 0) return KPSTM_ERR_INVALID_ARG;
     if (!c->d_lgeom) return KPSTM_ERR_STATE;
     const int ns = c->p.ns;
@@ -1764,6 +1800,7 @@ extern "C" int kpstm_lsm_cg(kpstm_ctx *c, const float *d_data, int32_t niter, fl
         double rr = 0.0;
         if ((st = dot(c, r, r, nd, &rr))) break;
         if (resid) resid[0] = sqrt(rr);
+        if (niter == 0) break; /* m = 0 is the answer; no search direction is needed */
         if ((st = adjoint_r(sv))) break;
         if (cudaMemcpyAsync(pv, sv, sizeof(float) * nm, cudaMemcpyDeviceToDevice, c->cs) != cudaSuccess) {
             st = KPSTM_ERR_CUDA;
@@ -1779,9 +1816,16 @@ extern "C" int kpstm_lsm_cg(kpstm_ctx *c, const float *d_data, int32_t niter, fl
             k_axpby<<<1024, 256, 0, c->cs>>>(d_model, pv, (float)alpha, 1.0f, nm);
             k_axpby<<<1024, 256, 0, c->cs>>>(r, q, (float)(-alpha), 1.0f, nd);
             if ((st = store_r())) break;
-            if (resid) {
+            if (resid || monitor) {
                 if ((st = dot(c, r, r, nd, &rr))) break;
-                resid[it + 1] = sqrt(rr);
+                if (resid) resid[it + 1] = sqrt(rr);
+            }
+            if (monitor) {
+                if (cudaGetLastError() != cudaSuccess) {
+                    st = KPSTM_ERR_CUDA;
+                    break;
+                }
+                if (monitor(it + 1, d_model, sqrt(rr), user)) break; /* the caller's stop */
             }
             if (it + 1 == niter) { /* x and r are final; the next direction (one L^T) is never used */
                 if (cudaGetLastError() != cudaSuccess) st = KPSTM_ERR_CUDA;

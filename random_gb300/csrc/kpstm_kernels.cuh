@@ -838,7 +838,12 @@ struct KpDemigArgs {
     unsigned long long *acc;       /* [nlive][ng] zeroed fixed-point rows in L2 (k_demig<false>); null when the rows are in shared memory */
     int *status;
     int nx, ny, ncls, ns, ng;      /* ng: accumulator entries per trace, ns + tm - 1 */
-    int shift;                     /* bound pass: extra halvings of its scale (large images) */
+    int bound_g;                   /* bound pass: |gs| < 2^bound_g */
+    int limb_r;                    /* SH rows: G = hi 2^limb_r + lo */
+    int norm_cols;                 /* SH rows: columns between limb normalisations */
+    float tailf;                   /* the pairs' float-position tails, as a fraction of (L 1) */
+    const float *wbound;           /* [nlive] largest weight x t/(8 dt) of the trace's pairs (bound pass) */
+    float *wbound_out;             /* bound pass: receives wbound */
     float ax0, adx, ay0, ady;      /* column coordinates: IX(xc) ~ ax0 + xc adx */
     double aperture;
     float aperture_f;              /* as KpImageArgs */
@@ -878,19 +883,6 @@ __device__ __forceinline__ void kp_red_add_u64(unsigned long long *p, unsigned l
 
 #define KP_DM_NONE (-(1 << 29)) /* entry index of a lane without a pair */
 
-/* Exact 64-bit add in shared memory from two native 32-bit shared atomics:
-   the low word's add returns the word before it, which tells whether this
-   add carried out of it; the high word receives the high half plus that
-   carry.  Concurrent adds to one entry each see their own predecessor, so
-   the pair of words always holds the exact sum modulo 2^64. */
-__device__ __forceinline__ void kp_sadd_u64(unsigned long long *p, unsigned long long v)
-{
-    unsigned int *wd = reinterpret_cast<unsigned int *>(p); /* [0] low word, [1] high word */
-    const unsigned int lo = (unsigned int)v, hi = (unsigned int)(v >> 32);
-    const unsigned int old = atomicAdd(&wd[0], lo);
-    atomicAdd(&wd[1], hi + (old + lo < old ? 1u : 0u));
-}
-
 /* RN(x) as an int64 for |x| <= 2^45 with fp32 and integer operations only
    (__float2ll_rn runs on the FP64 pipe, slow on this GPU): x = qh 2^23 + r
    exactly with qh = RN(x 2^-23) and |r| <= 2^22; both roundings are the
@@ -905,36 +897,29 @@ __device__ __forceinline__ long long kp_f2ll_rn45(float x)
     return (long long)qh * 8388608LL + (long long)ql;
 }
 
-/* One tap of the transpose for the 32 lanes of a warp (consecutive samples):
-   e0 at entry n, e1 at n + 1 (entries < 0 dropped).  Where the next lane's
-   n is this lane's n + 1 - the usual case, the traveltime advancing by about
-   a sample per sample - this lane's e1 is handed to it with a shuffle and
-   added to its e0, so one 64-bit add per lane and tap is issued instead of
-   two.  All lanes must call it.  SH: G is the warp's row in shared memory
-   (kp_sadd_u64), else the trace's row in global memory (RED to L2). */
-template <bool SH>
-__device__ __forceinline__ void kp_demig_tap(unsigned long long *G, int n, long long e0, long long e1, int lane)
+/* RN(x) as the limb pair h 2^R + l of the shared-memory rows:
+   h = RN(x 2^-R) and l = RN(x - h 2^R), |l| <= 2^(R-1), for |x| < 2^(22+R)
+   and R <= 21.  x 2^-R is exact and the 1.5 * 2^23 shift rounds it to an
+   integer; x - h 2^R is exact in one fma (it is a multiple of x's spacing
+   and at most 2^(R-1) in size); the second shift rounds that to an integer,
+   and h 2^R + l = RN(x) because h 2^R is an integer.  Six FMA-pipe/ALU
+   operations, no conversion instruction. */
+__device__ __forceinline__ void kp_split(float x, float sR, float nR, int &h, int &l)
 {
-    const int np = __shfl_up_sync(0xffffffffu, n, 1);
-    const long long e1p = __shfl_up_sync(0xffffffffu, e1, 1);
-    const int nn = __shfl_down_sync(0xffffffffu, n, 1);
-    if (lane > 0 && np + 1 == n) e0 += e1p;         /* the previous lane's e1 lands here */
-    const bool keep1 = !(lane < 31 && nn == n + 1); /* else the next lane takes it */
-    if (SH) {
-        if (n >= 0) kp_sadd_u64(&G[n], (unsigned long long)e0);
-        if (keep1 && n >= -1) kp_sadd_u64(&G[n + 1], (unsigned long long)e1);
-    } else {
-        if (n >= 0) kp_red_add_u64(&G[n], (unsigned long long)e0);
-        if (keep1 && n >= -1) kp_red_add_u64(&G[n + 1], (unsigned long long)e1);
-    }
+    const float sh = __fmaf_rn(x, sR, KP_MAGIC);
+    h = __float_as_int(sh) - KP_MAGIC_BITS;
+    const float lf = __fmaf_rn(__fadd_rn(sh, -KP_MAGIC), nR, x);
+    l = __float_as_int(__fadd_rn(lf, KP_MAGIC)) - KP_MAGIC_BITS;
 }
 
-/* Dynamic shared memory of k_demig: t2[ns] and ts[ns], then (SH) one 64-bit
-   accumulator row of ngp = ng rounded up to even entries per warp. */
+/* Dynamic shared memory of k_demig: t2[ns] and ts[ns], then (SH) one
+   accumulator row per warp: ngp int32 low limbs followed by ngp int32 high
+   limbs (ngp = ng rounded up to a multiple of 4). */
+__host__ __device__ inline int kp_demig_ngp(int ng) { return (ng + 3) & ~3; }
 __host__ __device__ inline size_t kp_demig_smem(int ns, int ng, bool sh)
 {
-    const size_t head = sizeof(float) * 2 * (size_t)((ns + 1) & ~1);
-    return head + (sh ? (size_t)KP_DM_WARPS * (size_t)((ng + 1) & ~1) * sizeof(unsigned long long) : 0);
+    const size_t head = sizeof(float) * 2 * (size_t)((ns + 3) & ~3);
+    return head + (sh ? (size_t)KP_DM_WARPS * 2 * (size_t)kp_demig_ngp(ng) * sizeof(int) : 0);
 }
 
 /* Demigration d = L m, the exact transpose of the full-mode migration of
@@ -947,35 +932,44 @@ __host__ __device__ inline size_t kp_demig_smem(int ns, int ng, bool sh)
    c g f at n + 1, g = weight x t/(8 dt) x m - six entries per pair instead
    of the 2 Lf + 1 of an explicit triangle - and the trace is
    d[k] = sum_{i >= k} G[i] (i - k + 1), two reverse prefix sums.
-   Exactness: G is 64-bit fixed point, e1 = RN(c gs f), e0 = c Q - e1 with
+   Exactness: G is integer fixed point, e1 = RN(c gs f), e0 = c Q - e1 with
    Q = RN(gs), so each pair's entries sum to exactly zero and integer sums
-   carry no rounding into the prefix sums.  The per-trace scale 2^E keeps
-   |d| 2^E < 2^61 from |L m| <= max|m| (L 1) (L has non-negative
-   coefficients); (L 1) per trace comes from a bound pass of this kernel on
-   the all-ones model with the conservative scale |gs| < 2^30 (weight x
-   t/(8 dt) <= 2/dt).  The result is deterministic.
-   SH (the row fits in shared memory): each warp accumulates its trace in
-   its own 64-bit row in shared memory with exact two-word shared atomics
-   (kp_sadd_u64) and takes the prefix sums there; L2 sees no atomics.  Else
-   the entries are added with fire-and-forget 64-bit atomics (RED) into the
-   trace's row in global memory, which stays in L2 while the warp works on
-   it.  The float -> int64 roundings use kp_f2ll_rn45 (no FP64 pipe); the
-   scale keeps their arguments below 2^45. */
+   carry no rounding into the prefix sums.  The per-trace scale 2^E follows
+   from |L m| <= max|m| (L 1) (L has non-negative coefficients), (L 1) per
+   trace from a bound pass of this kernel on the all-ones model, which also
+   records the trace's largest pair weight.  The result is deterministic.
+   SH (the rows fit in shared memory): each entry is two int32 limbs, G[n] =
+   hi[n] 2^R + lo[n], in two planar rows of the warp (consecutive entries in
+   consecutive banks); an entry is added as two returnless 32-bit shared
+   atomics with no carry between them.  Every a.norm_cols columns the warp
+   moves each lo limb's multiple of 2^R into hi.  Bounds (the host picks R
+   and the bound pass's scale): an entry receives at most 4 units of 2^(R-1)
+   per sample of a column (coefficients 1, -2, 1; coinciding neighbour
+   entries), so lo stays within 2^31 for 4 ns norm_cols + 1 units; every
+   partial sum of an entry is a second difference of a partial trace,
+   |G| <= 4 max|d|, and the scale keeps 4 max|d| 2^E + 2^31 below 2^(31+R).
+   At the end the two prefix sums run in int64 in place (each lane's chunk
+   of entries, the low and high words of each value stored back in the two
+   limbs).
+   Else (long rows) the entries are added with fire-and-forget 64-bit RED
+   into the trace's row in global memory, which stays in L2. */
 template <bool SH>
 __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigArgs a)
 {
     extern __shared__ __align__(16) float dm_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ns = a.ns, ng = a.ng, ngp = (ng + 1) & ~1;
-    float *s_t2 = dm_smem;      /* [ns] (t/2)^2 */
-    float *s_ts = dm_smem + ns; /* [ns] t/(8 dt) */
-    unsigned long long *s_rows = reinterpret_cast<unsigned long long *>(dm_smem + ((ns + 1) & ~1) * 2);
+    const int ns = a.ns, ng = a.ng, ngp = kp_demig_ngp(ng);
+    const int nsp = (ns + 3) & ~3;
+    float *s_t2 = dm_smem;       /* [ns] (t/2)^2 */
+    float *s_ts = dm_smem + nsp; /* [ns] t/(8 dt) */
+    int *s_lo = reinterpret_cast<int *>(dm_smem + 2 * nsp) + (size_t)w * 2 * ngp;
+    int *s_hi = s_lo + ngp;
     for (int k = threadIdx.x; k < ns; k += blockDim.x) {
         s_t2[k] = a.t2c[k].x;
         s_ts[k] = a.tscale[k];
     }
     if (SH)
-        for (int i = lane; i < ngp; i += 32) s_rows[(size_t)w * ngp + i] = 0ull;
+        for (int i = lane; i < 2 * ngp; i += 32) s_lo[i] = 0;
     __syncthreads();
     const bool bound = a.model == nullptr;
     const unsigned int mb = bound ? __float_as_uint(1.0f) : *a.absmax;
@@ -988,26 +982,41 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
     if (wi >= *a.nlive) return; /* no block barrier below */
     const int slot = a.order ? a.order[wi] : wi;
     const float bw = 2.002f / a.dt; /* >= weight x t/(8 dt) over all pairs */
+    const int R = a.limb_r;
     int E;
     if (bound) {
-        E = 29 - (ilogbf(bw) + 1) - a.shift; /* |gs| < 2^30 */
+        E = a.bound_g - (ilogbf(bw) + 1); /* |gs| < 2^bound_g */
+    } else if (SH) {
+        /* Limb rows.  max|d| 2^E <= 2^E max|m| ((L 1) + tails) with (L 1) from the
+           bound pass (its own fixed point costs < 1%: a factor 2 covers it) and
+           the tails at most tailf (L 1): 2^E max|m| (1 + tailf) (L 1) < 2^(27+R)
+           keeps 4 max|d| 2^E + 2^31 < 2^(31+R).  The split needs |x| <= 2 |gs|
+           < 2^(22+R), |gs| <= 2^E max|m| wmax (1 + 2^-20), wmax the trace's
+           largest weight x t/(8 dt) from the bound pass. */
+        const float mm = __uint_as_float(mb);
+        const float v = mm * a.dbound[slot] * (1.0f + a.tailf);
+        const float wv = mm * fminf(a.wbound[slot] * 1.001f, bw);
+        E = min(v > 0.0f ? 27 + R - (ilogbf(fminf(v, 3.0e38f)) + 1) : 127,
+                wv > 0.0f ? 21 + R - (ilogbf(fminf(wv, 3.0e38f)) + 1) : 127);
     } else {
-        /* 2^E max|m| max(2 (L 1), 2 bw) < 2^61, and |2 gs| <= 2 bw max|m| 2^E < 2^45
-           for kp_f2ll_rn45 */
-        const float v = __uint_as_float(mb) * fmaxf(2.0f * a.dbound[slot], 2.0f * bw);
+        /* 2^E max|m| max(2 (1 + tailf) (L 1), 2 bw) < 2^61, and |2 gs| < 2^45 for kp_f2ll_rn45 */
+        const float v = __uint_as_float(mb) * fmaxf(2.0f * (1.0f + a.tailf) * a.dbound[slot], 2.0f * bw);
         E = min(61 - (ilogbf(fminf(v, 3.0e38f)) + 1),
                 43 - ilogbf(fminf(__uint_as_float(mb) * bw, 3.0e38f)));
     }
     E = max(-126, min(127, E));
     const float scale = __int_as_float((E + 127) << 23);
     const float inv = ldexpf(1.0f, -E);
+    const float sR = ldexpf(1.0f, -R), nR = -ldexpf(1.0f, R);
 
     const kpstm_geom g = a.geom[slot];
     const int cls = g.cls;
-    unsigned long long *Gg = SH ? s_rows + (size_t)w * ngp : a.acc + (int64_t)slot * ng;
+    unsigned long long *Gg = SH ? nullptr : a.acc + (int64_t)slot * ng;
     const float apm = (float)a.aperture * 1.00001f + 1.0f; /* range margin; exact test below */
     const int x_lo = max(0, (int)floorf((g.cmpx - apm - a.ax0) / a.adx) - 1);
     const int x_hi = min(a.nx - 1, (int)ceilf((g.cmpx + apm - a.ax0) / a.adx) + 1);
+    int since_norm = 0;
+    float wmax = 0.0f; /* bound pass: largest weight x t/(8 dt) */
     for (int xc = x_lo; xc <= x_hi; ++xc) {
         const float dxc = fmaf((float)xc, a.adx, a.ax0) - g.cmpx;
         const float rem = apm * apm - dxc * dxc;
@@ -1027,6 +1036,19 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
                 kp_fail(a.status, KPSTM_ERR_VELOCITY_RANGE);
                 continue;
             }
+            if (SH && since_norm == a.norm_cols) {
+                /* each lo limb keeps its centred remainder mod 2^R, hi takes the rest */
+                __syncwarp();
+                for (int i = lane; i < ng; i += 32) {
+                    const int lo = s_lo[i];
+                    const int q = (lo + (1 << (R - 1))) >> R;
+                    s_lo[i] = lo - (q << R);
+                    s_hi[i] += q;
+                }
+                __syncwarp();
+                since_norm = 0;
+            }
+            ++since_norm;
             float sx = __fsub_rn(IX, g.sxt), sy = __fsub_rn(IY, g.syt);
             float gx = __fsub_rn(IX, g.gxt), gy = __fsub_rn(IY, g.gyt);
             const float dIS2 = __fadd_rn(__fmul_rn(sx, sx), __fmul_rn(sy, sy));
@@ -1055,8 +1077,9 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
                     if (!__any_sync(0xffffffffu, ok)) continue; /* warp-uniform */
                     float Lf, wgt;
                     kp_pair_width(rs, rr, axs, axr, ays, ayr, tv.y, a.lmaxf, Lf, wgt);
-                    const float gs = ok ? __fmul_rn(__fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u])), scale) : 0.0f;
-                    const long long Q = kp_f2ll_rn45(gs);
+                    const float wts = __fmul_rn(wgt, __fmul_rn(s_ts[tt], mv[u]));
+                    if (bound && ok) wmax = fmaxf(wmax, wts);
+                    const float gs = ok ? __fmul_rn(wts, scale) : 0.0f;
                     /* the positions exactly as k_image computes them: y = Tf, Tf +- Lf,
                        P index n = floor(y) - 1, fraction y - floor(y) */
                     const float y0 = ok ? Tf : 1.0f, ya = y0 + Lf, yb = y0 - Lf;
@@ -1064,12 +1087,51 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
                     const float fa = ya - (__int_as_float(ba) - KP_MAGIC);
                     const float fb = yb - (__int_as_float(bb) - KP_MAGIC);
                     const float f0 = y0 - (__int_as_float(b00) - KP_MAGIC);
-                    const long long a1 = kp_f2ll_rn45(__fmul_rn(gs, fa));
-                    const long long b1 = kp_f2ll_rn45(__fmul_rn(gs, fb));
-                    const long long c1 = kp_f2ll_rn45(__fmul_rn(-2.0f * gs, f0));
-                    kp_demig_tap<SH>(Gg, ok ? ba - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - a1, a1, lane);
-                    kp_demig_tap<SH>(Gg, ok ? bb - KP_MAGIC_BITS - 1 : KP_DM_NONE, Q - b1, b1, lane);
-                    kp_demig_tap<SH>(Gg, ok ? b00 - KP_MAGIC_BITS - 1 : KP_DM_NONE, -2 * Q - c1, c1, lane);
+                    const int na = ba - KP_MAGIC_BITS - 1, nb = bb - KP_MAGIC_BITS - 1;
+                    const int n0 = b00 - KP_MAGIC_BITS - 1;
+                    if (SH) {
+                        int qh, ql, h1, l1;
+                        kp_split(gs, sR, nR, qh, ql);
+                        /* tap at ya (c = 1): e1 = RN(gs fa) at na + 1, e0 = Q - e1 at na */
+                        kp_split(__fmul_rn(gs, fa), sR, nR, h1, l1);
+                        if (ok && na >= 0) {
+                            atomicAdd(s_lo + na, ql - l1);
+                            atomicAdd(s_hi + na, qh - h1);
+                        }
+                        if (ok && na >= -1) {
+                            atomicAdd(s_lo + na + 1, l1);
+                            atomicAdd(s_hi + na + 1, h1);
+                        }
+                        kp_split(__fmul_rn(gs, fb), sR, nR, h1, l1); /* tap at yb (c = 1) */
+                        if (ok && nb >= 0) {
+                            atomicAdd(s_lo + nb, ql - l1);
+                            atomicAdd(s_hi + nb, qh - h1);
+                        }
+                        if (ok && nb >= -1) {
+                            atomicAdd(s_lo + nb + 1, l1);
+                            atomicAdd(s_hi + nb + 1, h1);
+                        }
+                        kp_split(__fmul_rn(-2.0f * gs, f0), sR, nR, h1, l1); /* tap at y0 (c = -2) */
+                        if (ok && n0 >= 0) {
+                            atomicAdd(s_lo + n0, -2 * ql - l1);
+                            atomicAdd(s_hi + n0, -2 * qh - h1);
+                        }
+                        if (ok && n0 >= -1) {
+                            atomicAdd(s_lo + n0 + 1, l1);
+                            atomicAdd(s_hi + n0 + 1, h1);
+                        }
+                    } else {
+                        const long long Q = kp_f2ll_rn45(gs);
+                        const long long a1 = kp_f2ll_rn45(__fmul_rn(gs, fa));
+                        const long long b1 = kp_f2ll_rn45(__fmul_rn(gs, fb));
+                        const long long c1 = kp_f2ll_rn45(__fmul_rn(-2.0f * gs, f0));
+                        if (ok && na >= 0) kp_red_add_u64(&Gg[na], (unsigned long long)(Q - a1));
+                        if (ok && na >= -1) kp_red_add_u64(&Gg[na + 1], (unsigned long long)a1);
+                        if (ok && nb >= 0) kp_red_add_u64(&Gg[nb], (unsigned long long)(Q - b1));
+                        if (ok && nb >= -1) kp_red_add_u64(&Gg[nb + 1], (unsigned long long)b1);
+                        if (ok && n0 >= 0) kp_red_add_u64(&Gg[n0], (unsigned long long)(-2 * Q - c1));
+                        if (ok && n0 >= -1) kp_red_add_u64(&Gg[n0 + 1], (unsigned long long)c1);
+                    }
                 }
             }
         }
@@ -1077,22 +1139,31 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
     /* order the row's atomics before the warp reads it back (past L1) */
     if (!SH) __threadfence();
     __syncwarp();
-    /* the row's entries: shared memory (SH), or L2 past L1 */
-    auto ldg = [&](int i) -> unsigned long long {
-        if constexpr (SH) return Gg[i];
+    /* d = two reverse prefix sums of G in int64, lane l owning entries
+       [l C, l C + C).  SH: pass 1 reads the limb form hi 2^R + lo and both
+       passes store each int64 as its low word (lo row) and high word (hi
+       row); else the row is int64 in L2. */
+    auto ldA = [&](int i) -> unsigned long long {
+        if constexpr (SH) return ((unsigned long long)(long long)s_hi[i] << R) + (unsigned long long)(long long)s_lo[i];
         else return __ldcg(&Gg[i]);
     };
-    auto stg = [&](int i, unsigned long long v) {
-        if constexpr (SH) Gg[i] = v;
-        else __stcg(&Gg[i], v);
+    auto ldB = [&](int i) -> unsigned long long {
+        if constexpr (SH) return ((unsigned long long)(unsigned int)s_hi[i] << 32) | (unsigned int)s_lo[i];
+        else return __ldcg(&Gg[i]);
     };
-    /* d = two reverse prefix sums of G, in place in the row, lane l owning
-       entries [l C, l C + C) */
+    auto stB = [&](int i, unsigned long long v) {
+        if constexpr (SH) {
+            s_lo[i] = (int)(unsigned int)v;
+            s_hi[i] = (int)(unsigned int)(v >> 32);
+        } else {
+            __stcg(&Gg[i], v);
+        }
+    };
     const int C = (ng + 31) >> 5;
     const int lo = min(ng, lane * C), hi = min(ng, lo + C);
     for (int pass = 0; pass < 2; ++pass) {
         unsigned long long tot = 0ull;
-        for (int i = lo; i < hi; ++i) tot += ldg(i);
+        for (int i = lo; i < hi; ++i) tot += pass ? ldB(i) : ldA(i);
         unsigned long long incl = tot; /* sum over lanes >= lane */
         for (int d = 1; d < 32; d <<= 1) {
             const unsigned long long v = __shfl_down_sync(0xffffffffu, incl, d);
@@ -1100,19 +1171,25 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
         }
         unsigned long long run = incl - tot;
         for (int i = hi - 1; i >= lo; --i) {
-            run += ldg(i);
-            stg(i, run);
+            run += pass ? ldB(i) : ldA(i);
+            stB(i, run);
         }
     }
     __syncwarp(); /* the lanes' rows are visible to the whole warp */
-    float dmax = 0.0f;
     if (bound) {
-        for (int k = lane; k < ns; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)ldg(k)) * inv));
+        /* the bound covers every entry of the row (the partial sums of all of
+           them must fit), not only the samples that are output */
+        float dmax = 0.0f;
+        for (int k = lane; k < ng; k += 32) dmax = fmaxf(dmax, fabsf(__ll2float_rn((long long)ldB(k)) * inv));
         dmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dmax)));
-        if (lane == 0) a.dbound_out[slot] = dmax;
+        wmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(wmax)));
+        if (lane == 0) {
+            a.dbound_out[slot] = dmax;
+            a.wbound_out[slot] = wmax;
+        }
     } else {
         float *o = a.out + (int64_t)g.src * ns;
-        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)ldg(k)), inv);
+        for (int k = lane; k < ns; k += 32) o[k] = __fmul_rn(__ll2float_rn((long long)ldB(k)), inv);
     }
 }
 

@@ -152,10 +152,29 @@ class Migration:
         capi.check("kpstm_lsm_pair_count", self._lib.kpstm_lsm_pair_count(self._h, C.byref(v)))
         return v.value
 
-    def lsm_cg(self, d_data: int, niter: int, d_model: int) -> np.ndarray:
-        resid = np.zeros(niter + 1, np.float64)
-        capi.check("kpstm_lsm_cg", self._lib.kpstm_lsm_cg(self._h, d_data, niter, d_model, resid.ctypes.data))
-        return resid
+    def lsm_cg(self, d_data: int, niter: int, d_model: int, monitor=None) -> np.ndarray:
+        """CGLS from m = 0 (kpstm_lsm_cg_ex).  ``monitor(k, d_model_ptr, resid_k)``,
+        if given, runs after iteration k has updated the model; a truthy
+        return ends the solve there.  Returns the residual norms reached."""
+        resid = np.full(niter + 1, np.nan, np.float64)
+        if monitor is None:
+            capi.check("kpstm_lsm_cg", self._lib.kpstm_lsm_cg(self._h, d_data, niter, d_model, resid.ctypes.data))
+            return resid
+        err = []
+
+        def _cb(k, ptr, res, _user):
+            try:
+                return 1 if monitor(int(k), int(ptr or 0), float(res)) else 0
+            except BaseException as e:  # a Python error must not unwind through C
+                err.append(e)
+                return 1
+
+        cb = capi.CG_MONITOR(_cb)
+        st = self._lib.kpstm_lsm_cg_ex(self._h, d_data, niter, d_model, resid.ctypes.data, cb, None)
+        if err:
+            raise err[0]
+        capi.check("kpstm_lsm_cg_ex", st)
+        return resid[~np.isnan(resid)]
 
     def synchronize(self) -> None:
         capi.check("kpstm_synchronize", self._lib.kpstm_synchronize(self._h))

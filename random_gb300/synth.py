@@ -342,6 +342,63 @@ def patch3d(ntr: int, **kw) -> Survey:
     return s
 
 
+def reflectivity_model(nx: int = 200, ny: int = 200, ns: int = 751, dt: float = 0.004, bin_m: float = 25.0,
+                       n_refl: int = 12, n_scat: int = 100, seed: int = 5,
+                       v_law=(1600.0, 500.0, 100.0, 8000.0), x0: float = 0.0) -> np.ndarray:
+    """Reflectivity model of the least-squares workload on the image grid,
+    float32 [nx, ny, 1, ns] (stack layout): ``n_refl`` planar dipping
+    reflectors and ``n_scat`` point scatterers, seeded.
+
+    A reflector has a centre time t0c ~ U(0.3, 0.85 T) (T the record
+    length), a dip theta ~ U(0, 30 deg) along an azimuth ~ U(0, 2 pi) and an
+    amplitude ~ +-U(0.5, 1); in every column it is one spike at the
+    zero-offset time t0c + 2 tan(theta)/v (lateral distance from the model
+    centre), v = v_rms at t0c, split linearly between the two samples around
+    it.  A scatterer is a spike of amplitude +-U(0.5, 1) at a random column
+    and time ~ U(0.3, 0.9 T).  ``x0`` is the coordinate of column 0 (for
+    the lateral velocity term)."""
+    rng = np.random.default_rng(seed)
+    T = (ns - 1) * dt
+    v0, vt, va, lam = v_law
+    m = np.zeros((nx, ny, 1, ns), np.float64)
+    X, Y = np.meshgrid(np.arange(nx) * bin_m, np.arange(ny) * bin_m, indexing="ij")
+    xc, yc = 0.5 * (nx - 1) * bin_m, 0.5 * (ny - 1) * bin_m
+    t0c = rng.uniform(0.3, 0.85 * T, n_refl)
+    dip = np.radians(rng.uniform(0.0, 30.0, n_refl))
+    az = rng.uniform(0.0, 2.0 * math.pi, n_refl)
+    amp = rng.uniform(0.5, 1.0, n_refl) * rng.choice([-1.0, 1.0], n_refl)
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    for k in range(n_refl):
+        v = v0 + vt * t0c[k] + va * math.sin(2.0 * math.pi * (x0 + xc) / lam)
+        p = 2.0 * math.tan(dip[k]) / v
+        t0 = t0c[k] + p * (math.cos(az[k]) * (X - xc) + math.sin(az[k]) * (Y - yc))
+        tau = t0 / dt
+        ok = (tau >= 1.0) & (tau < ns - 2)
+        n0 = np.floor(tau[ok]).astype(np.int64)
+        f = tau[ok] - n0
+        np.add.at(m, (ix[ok], iy[ok], 0, n0), amp[k] * (1.0 - f))
+        np.add.at(m, (ix[ok], iy[ok], 0, n0 + 1), amp[k] * f)
+    sx = rng.integers(0, nx, n_scat)
+    sy = rng.integers(0, ny, n_scat)
+    st = np.rint(rng.uniform(0.3, 0.9 * T, n_scat) / dt).astype(np.int64)
+    sa = rng.uniform(0.5, 1.0, n_scat) * rng.choice([-1.0, 1.0], n_scat)
+    np.add.at(m, (sx, sy, 0, st), sa)
+    return m.astype(np.float32)
+
+
+def lsm_survey_model(ntr: int = 250_000, nx: int = 200, ny: int = 200, ns: int = 751, dt: float = 0.004,
+                     seed: int = 5, **kw) -> Patch3DModel:
+    """Acquisition of the least-squares workload: ``ntr`` traces with
+    midpoints uniform over the nx x ny model at 25 m, offsets U(0, 3000 m),
+    random azimuths, ns samples at ``dt``; aperture 3000 m, full physics,
+    stack output.  Its data are d = L m (+ noise), not the events of
+    patch3d_model."""
+    base = dict(ns=ns, dt=dt, nx=nx, ny=ny, bin_m=25.0, max_offset=3000.0, n_refl=0, n_diff=0, freq=25.0,
+                aperture=3000.0, seed=seed, mode=1, output=1, name="lsm")
+    base.update(kw)
+    return patch3d_model(ntr, **base)
+
+
 def offset_bin_counts(nbins: int = 64, mean: float = 15000.0, lo: int = 2000, hi: int = 40000,
                       seed: int = 4) -> np.ndarray:
     """Traces per offset bin of the batched offset-class workload:

@@ -135,3 +135,37 @@ def test_cg_against_fp64_oracle(kpstm_lib, oracle_lib, precision):
     assert np.all(np.diff(res) <= 1e-6 * res[0])          # residual never grows
     err = rel_l2(x, x64)
     assert err <= (1e-3 if precision == capi.PREC_FP32 else 2e-2), err
+
+
+def test_cg_monitor_iterates_and_stop(kpstm_lib):
+    """kpstm_lsm_cg_ex: the iterate the monitor sees after iteration k equals
+    a separate k-iteration solve bit for bit (CGLS from m = 0 is the same
+    recurrence), residuals agree, and a truthy return ends the solve."""
+    torch = pytest.importorskip("torch")
+    s = _survey(ntr=180, nx=6, ny=5)
+    rng = np.random.default_rng(5)
+    d = torch.as_tensor(rng.normal(size=(s.ntr, s.ns)).astype(np.float32)).cuda()
+    with Migration(dict(s.params, precision=capi.PREC_BF16_KAHAN), s.velocity) as mg:
+        mg.lsm_geometry(s.headers)
+        xm = torch.empty(mg.shape, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        seen, res_seen = [], []
+
+        def mon(k, ptr, res):
+            assert ptr == xm.data_ptr()
+            seen.append(xm.cpu().numpy().copy())
+            res_seen.append(res)
+            return False
+        resid = mg.lsm_cg(d.data_ptr(), 4, xm.data_ptr(), monitor=mon)
+        assert len(seen) == 4 and len(resid) == 5
+        assert np.allclose(res_seen, resid[1:], rtol=0, atol=0)
+        for k in (1, 3):
+            r2 = mg.lsm_cg(d.data_ptr(), k, xm.data_ptr())
+            assert np.array_equal(xm.cpu().numpy(), seen[k - 1])
+            assert np.array_equal(r2, resid[:k + 1])
+        stop = []
+        r3 = mg.lsm_cg(d.data_ptr(), 6, xm.data_ptr(), monitor=lambda k, p, r: stop.append(k) or k == 2)
+        assert stop == [1, 2] and len(r3) == 3
+        assert np.array_equal(xm.cpu().numpy(), seen[1])
+        r0 = mg.lsm_cg(d.data_ptr(), 0, xm.data_ptr())
+        assert len(r0) == 1 and not np.any(xm.cpu().numpy())
