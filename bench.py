@@ -349,6 +349,12 @@ def run_ours(args, rank, world, local_rank):
                                 "full_bf16" if args.precision == "bf16" else "full",
                                 table_rows=block, row_bytes=row_floats * 4)
     roofline["image_kernel_share"] = round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4)
+    # live pairs: those whose traveltime falls inside the trace (the fold
+    # counts), against all counted (trace, column, sample) pairs so far
+    _, fold = m.accumulators()
+    live = float(np.sum(fold.astype(np.float64) - 1.0))
+    live_fraction = live / max(1, m.pairs())
+    del fold
     del m
 
     # -------- e2e through the C ABI from pinned host memory
@@ -404,6 +410,12 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": int(prof["image_launches"] + prof["other_launches"]),
             "pairs": int(pairs_all), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "profile_ms": {"image": round(prof["image_ms"], 3), "prep": round(prof["prep_ms"], 3)},
+            "live_pair_fraction": round(live_fraction, 4),
+            "trace_storage": {"bytes_per_trace": NS * (2 if args.precision == "bf16" else 4) +
+                              (4 if args.precision == "bf16" else 0),
+                              "gb_per_s": round(block * (NS * (2 if args.precision == "bf16" else 4)) /
+                                                (elapsed_max / args.steps) / 1e9, 4),
+                              "note": "stored trace bytes of a step / step time"},
         }
         print(json.dumps(line), flush=True)
 
@@ -475,20 +487,58 @@ def run_offset_bins(args):
     print(json.dumps(line), flush=True)
 
 
+def cpu_line(nprocs: int, opt: str = "-O3"):
+    """The reference's kirchhoff() on the full config-1 line: the compiled
+    Kirchhoff.c (MPI/FFTW stand-ins) with its image cut into nprocs slabs
+    along the line (number_mpi_jobsX = nprocs, Kirchhoff.c:280-300), one
+    process per slab, all started together; every slab reads all traces
+    (Kirchhoff.c:1276).  Returns the wall seconds until the last ends."""
+    from oracle import refbuild
+    from random_gb300 import synth
+    s = synth.line2d()
+    work = Path(tempfile.mkdtemp(prefix="kline_"))
+    try:
+        s.write_files(work / "data.segy", work / "vel.segy")
+        cfg = refbuild.RefConfig(**s.ref_config(jobs_x=nprocs, jobs_y=1))
+        binary = refbuild.compile(cfg, opt=opt, tag=f"line{nprocs}")
+        (work / "run" / "image_dir").mkdir(parents=True, exist_ok=True)
+        for name in ("data.segy", "vel.segy"):
+            os.symlink(work / name, work / "run" / name)
+        t0 = time.perf_counter()
+        procs = [subprocess.Popen([str(binary)], cwd=work / "run", stdout=subprocess.DEVNULL,
+                                  stderr=subprocess.DEVNULL, stdin=subprocess.DEVNULL,
+                                  env=dict(os.environ, KPSTM_REF_RANK=str(j), KPSTM_REF_SIZE=str(nprocs)))
+                 for j in range(nprocs)]
+        for p in procs:
+            p.wait()
+        secs = time.perf_counter() - t0
+        if any(p.returncode for p in procs):
+            raise RuntimeError("reference rank failed")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    return secs
+
+
 def run_line(args):
-    """The 2-D line: 200 CMPs x 48 offsets = 9,600 traces, 1001 samples at
-    4 ms, 48 offset classes x 200 columns, reference operator (bit-exact
-    accumulators).  The launch configuration is chosen by kpstm_autotune on
-    the line itself (a fresh context), as a job loop would on its first block.
-    A step images the whole line once (1.61e9 pairs) from device-resident
-    traces."""
+    """Config 1, the 2-D line: 200 CMPs x 48 offsets = 9,600 traces, 1001
+    samples at 4 ms, 48 offset classes x 200 columns, reference operator
+    (accumulators bit-exact to the reference).  The launch configuration is
+    chosen by kpstm_autotune on the line itself (a fresh context), as a job
+    loop would on its first block.  A step images the whole line once
+    (1.61e9 pairs) from device-resident traces.  e2e: the same job through
+    kpstm_add_traces from pinned host buffers and kpstm_finish (image and
+    fold to host) per step.  CPU: the compiled reference on one rank over
+    the whole line (the config's "1 MPI rank"), and on all host cores with
+    its own slab decomposition."""
     import torch
     from random_gb300 import build, segy, synth
     from random_gb300.migration import Migration
     build.build()
     dev = torch.device("cuda", 0)
+    peaks = load_peaks()
     s = synth.line2d()
-    d_hdr = torch.from_numpy(np.ascontiguousarray(segy.headers_be(s.headers))).to(dev)
+    hdr_np = np.ascontiguousarray(segy.headers_be(s.headers))
+    d_hdr = torch.from_numpy(hdr_np).to(dev)
     d_smp = torch.from_numpy(np.ascontiguousarray(s.samples)).to(dev)
     m = Migration(s.params, s.velocity)
     stream = torch.cuda.Stream(device=dev)
@@ -498,17 +548,92 @@ def run_line(args):
     def step(i):
         m.add_traces_device(d_hdr.data_ptr(), d_smp.data_ptr(), s.ntr)
 
-    mark = {}
-    elapsed, clk = _timed_steps(step, args.warmup, args.steps, stream,
-                                after_warmup=lambda: mark.setdefault("p0", m.pairs()))
+    for i in range(args.warmup):
+        step(i)
     m.synchronize()
+    p0 = m.pairs()
+    m.profile(True)
+    m.profile_read()
+    # each step timed on its own, L2 flushed (a 512 MB write) between steps
+    flush = torch.empty(128 << 20, dtype=torch.float32, device=dev)
+    clocks = ClockSampler(0)
+    clocks.start()
+    elapsed = 0.0
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(args.warmup + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        elapsed += e0.elapsed_time(e1) / 1e3
+    clk = clocks.stop()
+    del flush
+    mark = {"p0": p0}
+    m.synchronize()
+    prof = m.profile_read()
+    m.profile(False)
     pairs = m.pairs() - mark["p0"]
+    launch_cfg = m.launch_config()
+    launches = max(1, int(prof["image_launches"]))
+    t_launch = prof["image_ms"] / 1e3 / launches
+    ncol, ncls, ns = 200, 48, 1001
+    row = ns + 1 + 8  # tap row (reference mode) + geometry header, floats
+    b_alg = s.ntr * row * 4 + s.ntr * 32 + ncol * ncls * ns * 4 * 2 * 2 + ncol * ns * 8
+    roofline = imaging_roofline(pairs / args.steps, t_launch, b_alg, clk, peaks, dev, launch_cfg, "reference")
+    roofline["image_kernel_share"] = round(prof["image_ms"] / (elapsed * 1e3), 4)
+    del m
+
+    # e2e: host buffers in, finished image and fold out, every step a whole job
+    h_hdr = torch.from_numpy(hdr_np).pin_memory()
+    h_smp = torch.from_numpy(np.ascontiguousarray(s.samples)).pin_memory()
+    out = torch.empty((ncol, 1, ncls, ns), dtype=torch.float32).pin_memory()
+    fold = torch.empty_like(out).pin_memory()
+    m2 = Migration(s.params, s.velocity)
+    m2.set_launch(**launch_cfg)
+    for _ in range(args.warmup):
+        m2.reset()
+        m2.add_traces_ptr(h_hdr.data_ptr(), h_smp.data_ptr(), s.ntr)
+        m2.finish_ptr(out.data_ptr(), fold.data_ptr())
+    t0 = time.perf_counter()
+    pe = 0
+    for _ in range(args.steps):
+        m2.reset()
+        p0 = m2.pairs()
+        m2.add_traces_ptr(h_hdr.data_ptr(), h_smp.data_ptr(), s.ntr)
+        m2.finish_ptr(out.data_ptr(), fold.data_ptr())
+        pe += m2.pairs() - p0
+    t_e2e = time.perf_counter() - t0
+    del m2
+    e2e = {"value": round(pe / t_e2e / 1e9, 4), "unit": UNIT,
+           "h2d_bytes_per_step": int(hdr_np.nbytes + s.samples.nbytes),
+           "d2h_bytes_per_step": int(out.numel() * 4 * 2),
+           "note": "per step: kpstm_reset, kpstm_add_traces from pinned host buffers, kpstm_finish "
+                   "(image and fold to host); wall clock"}
+
+    cpu = None
+    if not args.no_cpu:
+        t1 = cpu_line(1)
+        cores = host_cores()
+        tn = cpu_line(cores)
+        ppj = pe / args.steps
+        cpu = {"value": round(ppj / t1 / 1e9, 4), "unit": UNIT, "cores": 1, "kind": "reference",
+               "sample": f"the whole line (9,600 traces, {ppj:.4g} pairs) by the reference kirchhoff() "
+                         f"(-O3 -ffast-math, MPI/FFTW stand-ins) on one rank: {t1:.2f} s",
+               "all_cores": {"value": round(ppj / tn / 1e9, 4), "cores": cores,
+                             "sample": f"the same line cut into {cores} slabs (number_mpi_jobsX = {cores}), "
+                                       f"one rank per core: {tn:.2f} s"}}
     line = {"workload": "line", "metric": METRIC, "value": round(pairs / elapsed / 1e9, 4), "unit": UNIT,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(elapsed / args.steps * 1e3, 3),
-            "dtype": "f32", "config": {"traces": int(s.ntr), "ns": 1001, "image": "200x1x48x1001",
-                                       "mode": "reference (bit-exact)", "launch": cfg,
-                                       "autotune_ms": round(tune_ms, 3)},
-            "pairs_per_step": pairs / args.steps, "clocks": clk}
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(elapsed / args.steps * 1e3, 3), "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded 2-D line: 20 point scatterers, 25 Hz Ricker, 20 dB noise)",
+            "config": {"workload": "config 1: 2-D line, 200 CMPs x 48 offsets = 9,600 traces x 1001 samples "
+                                   "@ 4 ms, 200 x 48 x 1001 offset gathers, aperture 1500 m, reference operator",
+                       "traces": int(s.ntr), "launch": cfg, "autotune_ms": round(tune_ms, 3),
+                       "l2": "flushed between timed steps (512 MB write); each step timed alone"},
+            "pairs_per_step": pairs / args.steps, "gpu_launches": int(prof["image_launches"] + prof["other_launches"]),
+            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk}
     print(json.dumps(line), flush=True)
 
 

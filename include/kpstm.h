@@ -321,6 +321,23 @@ int kpstm_lsm_pair_count(kpstm_ctx *ctx, int64_t *pairs);
 int kpstm_finish_noalloc(const kpstm_params *params, const float *d_km, const float *d_fold,
                          float *d_out, void *cuda_stream);
 
+/* ---- test hooks --------------------------------------------------------------- */
+/* No counterpart in the reference, which exits on every error
+   (Kirchhoff.c:462-467) and ignores short reads (:1280-1281).  They let
+   tests drive the error paths without faulting a device. */
+
+/* The stage waits of the imaging kernel give up after `polls` polls (0: at
+   once; default 4194304) and report KPSTM_ERR_TIMEOUT at the next
+   synchronising call; the kernel still waits, with the full bound, for its
+   own copies in flight before it returns, and kpstm_reset clears the
+   status.  Per context. */
+int kpstm_debug_wait_limit(kpstm_ctx *ctx, uint32_t polls);
+/* The nth device allocation from now (0: the next) made by kpstm_create or
+   by the staging buffers of kpstm_add_traces* fails as if the device were
+   out of memory (KPSTM_ERR_OUT_OF_MEMORY); -1 disarms.  Process-wide, one
+   shot. */
+int kpstm_debug_fail_alloc(int32_t nth);
+
 /* ---- stand-alone set-up helpers (host only) -------------------------------- */
 
 /* create_aliasfilter, Kirchhoff.c:380-441: trangeMax and the low-pass

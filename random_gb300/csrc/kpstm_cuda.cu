@@ -11,6 +11,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -65,6 +67,7 @@ struct kpstm_ctx {
     float2 *d_t2c;
     float *d_tscale;             /* full mode: per-sample read-out factor t dt/8 */
     double *d_c4, *d_c4r;
+    float2 *d_c4rw;              /* [ns + 2] the reciprocals of the precision-mode integral as double-word floats */
     float *d_h;
     float *d_invl2;
     /* image */
@@ -103,6 +106,7 @@ struct kpstm_ctx {
     float *d_rvdt;               /* demigration: [nrow][ns] 1/(v dt)^2 */
     int nrow;                    /* velocity rows of the slab */
     int dbound_ok;
+    uint32_t wait_polls;         /* imaging stage waits give up after this many polls */
     /* stream handling / profiling */
     cudaStream_t own_cs;
     int prof;
@@ -147,6 +151,30 @@ static void prof_end(kpstm_ctx *c, int i, int stage, int launches)
     cudaEventRecord(c->ev[i + 1], c->cs);
     c->evstage[i] = stage;
     c->evlaunches[i] = launches;
+}
+
+/* Device allocations of the set-up and of the staging buffers go through
+   kp_dmalloc, so that kpstm_debug_fail_alloc can make one of them fail. */
+static std::atomic<int> g_fail_alloc(-1);
+
+template <class T>
+static cudaError_t kp_dmalloc(T **p, size_t bytes)
+{
+    int n = g_fail_alloc.load();
+    while (n >= 0 && !g_fail_alloc.compare_exchange_weak(n, n - 1)) {
+    }
+    if (n == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc((void **)p, bytes);
+}
+
+extern "C" int kpstm_debug_fail_alloc(int32_t nth)
+{
+    if (nth < -1) return KPSTM_ERR_INVALID_ARG;
+    g_fail_alloc.store(nth);
+    return KPSTM_OK;
 }
 
 static int kp_free_all(kpstm_ctx *c);
@@ -428,15 +456,16 @@ static int grow_work(kpstm_ctx *c, int64_t ntr)
     c->d_scl16 = nullptr;
     c->cap = 0;
     int64_t n = ntr + ntr / 8 + 64;
-    KP_CUDA(cudaMalloc(&c->d_graw, sizeof(kpstm_geom) * n));
-    KP_CUDA(cudaMalloc(&c->d_geom, sizeof(kpstm_geom) * n));
-    KP_CUDA(cudaMalloc(&c->d_cls, sizeof(int32_t) * n));
-    KP_CUDA(cudaMalloc(&c->d_order, sizeof(int32_t) * n));
-    KP_CUDA(cudaMalloc(&c->d_table, sizeof(float) * c->row * n));
-    if (c->p.precision == KPSTM_PREC_BF16_KAHAN) {
-        KP_CUDA(cudaMalloc(&c->d_smp16, sizeof(uint16_t) * c->p.ns * n));
-        KP_CUDA(cudaMalloc(&c->d_scl16, sizeof(float) * n));
-    }
+    if (kp_dmalloc(&c->d_graw, sizeof(kpstm_geom) * n) != cudaSuccess ||
+        kp_dmalloc(&c->d_geom, sizeof(kpstm_geom) * n) != cudaSuccess ||
+        kp_dmalloc(&c->d_cls, sizeof(int32_t) * n) != cudaSuccess ||
+        kp_dmalloc(&c->d_order, sizeof(int32_t) * n) != cudaSuccess ||
+        kp_dmalloc(&c->d_table, sizeof(float) * c->row * n) != cudaSuccess)
+        return KPSTM_ERR_OUT_OF_MEMORY;
+    if (c->p.precision == KPSTM_PREC_BF16_KAHAN &&
+        (kp_dmalloc(&c->d_smp16, sizeof(uint16_t) * c->p.ns * n) != cudaSuccess ||
+         kp_dmalloc(&c->d_scl16, sizeof(float) * n) != cudaSuccess))
+        return KPSTM_ERR_OUT_OF_MEMORY;
     c->cap = n;
     return KPSTM_OK;
 }
@@ -454,10 +483,10 @@ static int grow_stage(kpstm_ctx *c, int64_t ntr)
     }
     c->scap = 0;
     int64_t n = ntr + ntr / 8 + 64;
-    for (int s = 0; s < 2; ++s) {
-        KP_CUDA(cudaMalloc(&c->d_hdr[s], sizeof(int32_t) * 60 * n));
-        KP_CUDA(cudaMalloc(&c->d_smp[s], sizeof(float) * c->p.ns * n));
-    }
+    for (int s = 0; s < 2; ++s)
+        if (kp_dmalloc(&c->d_hdr[s], sizeof(int32_t) * 60 * n) != cudaSuccess ||
+            kp_dmalloc(&c->d_smp[s], sizeof(float) * c->p.ns * n) != cudaSuccess)
+            return KPSTM_ERR_OUT_OF_MEMORY;
     c->scap = n;
     return KPSTM_OK;
 }
@@ -517,6 +546,7 @@ static int enqueue_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp,
     pa.table = c->d_table;
     pa.c4 = c->d_c4;
     pa.c4r = c->d_c4r;
+    pa.c4rw = c->d_c4rw;
     pa.row = c->row;
     pa.ns = p->ns;
     pa.tm = s->dims.trange_max;
@@ -601,6 +631,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
 
     kpstm_ctx *c = (kpstm_ctx *)calloc(1, sizeof(kpstm_ctx));
     if (!c) return KPSTM_ERR_OUT_OF_MEMORY;
+    c->wait_polls = KP_WAIT_POLLS;
     c->p = *params;
     c->s = s;
     cudaGetDevice(&c->device);
@@ -630,6 +661,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     int32_t *t1 = (int32_t *)malloc(sizeof(int32_t) * ns);
     double *c4 = (double *)malloc(sizeof(double) * ns);
     double *c4r = (double *)malloc(sizeof(double) * ns);
+    float2 *c4rw = (float2 *)malloc(sizeof(float2) * (ns + 2));
     float2 *t2c = (float2 *)malloc(sizeof(float2) * ns);
     float *tsc = (float *)malloc(sizeof(float) * ns);
     double *hd = (double *)malloc(sizeof(double) * ns);
@@ -639,7 +671,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     float invl2[64];
     int nrow = 0;
     do {
-        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !t2c || !tsc || !hd || !hf) {
+        if (!colxy || !colrow || !t2 || !t1 || !c4 || !c4r || !c4rw || !t2c || !tsc || !hd || !hf) {
             st = KPSTM_ERR_OUT_OF_MEMORY;
             break;
         }
@@ -655,6 +687,14 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             t2c[t] = make_float2(t > 0 ? (float)(0.25 * (double)t * (double)t) : 1e-12f,
                                  (float)((double)t / (8.0 * (double)params->dt)));
             tsc[t] = (float)((double)t / (8.0 * (double)params->dt)); /* t0/(8 dt^2), sample units */
+        }
+        /* 1/(4 t2[t]) for 0 < t < ns and 1/(dt t)^2 for the tail steps t = ns,
+           ns + 1 (Kirchhoff.c:1316-1320), as a float plus its remainder */
+        for (int t = 0; t < ns + 2; ++t) {
+            const double dtd = (double)params->dt;
+            const double r = t == 0 ? 0.0 : (t < ns ? 1.0 / c4[t] : 1.0 / (dtd * dtd * (double)t * (double)t));
+            const float rh = (float)r;
+            c4rw[t] = make_float2(rh, (float)(r - (double)rh));
         }
         st = kpstm_lowpass_kernel(params, hd);
         if (st) break;
@@ -722,7 +762,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             }
             size_t nimg = (size_t)s.nclass * ncol * ns;
 #define KP_ALLOC(ptr, bytes)                                                                                 \
-    if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess) {                                                        \
+    if (kp_dmalloc(&(ptr), (bytes)) != cudaSuccess) {                                                        \
         st = KPSTM_ERR_OUT_OF_MEMORY;                                                                        \
         break;                                                                                               \
     }
@@ -737,6 +777,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             if (params->mode == KPSTM_MODE_FULL) KP_ALLOC(c->d_tscale, sizeof(float) * ns);
             KP_ALLOC(c->d_c4, sizeof(double) * ns);
             KP_ALLOC(c->d_c4r, sizeof(double) * ns);
+            KP_ALLOC(c->d_c4rw, sizeof(float2) * (ns + 2));
             KP_ALLOC(c->d_h, sizeof(float) * ns);
             KP_ALLOC(c->d_invl2, sizeof(float) * 64);
             KP_ALLOC(c->d_km, sizeof(float) * nimg);
@@ -756,6 +797,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
             if (c->d_tscale) cudaMemcpyAsync(c->d_tscale, tsc, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_c4, c4, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_c4r, c4r, sizeof(double) * ns, cudaMemcpyHostToDevice, c->cs);
+            cudaMemcpyAsync(c->d_c4rw, c4rw, sizeof(float2) * (ns + 2), cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_h, hf, sizeof(float) * ns, cudaMemcpyHostToDevice, c->cs);
             cudaMemcpyAsync(c->d_invl2, invl2, sizeof(float) * 64, cudaMemcpyHostToDevice, c->cs);
             cudaMemsetAsync(c->d_km, 0, sizeof(float) * nimg, c->cs);
@@ -778,6 +820,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     free(t1);
     free(c4);
     free(c4r);
+    free(c4rw);
     free(t2c);
     free(tsc);
     free(hd);
@@ -798,7 +841,7 @@ static int kp_free_all(kpstm_ctx *c)
     if (c->cs) cudaStreamSynchronize(c->cs);
     if (c->own_cs && c->own_cs != c->cs) cudaStreamSynchronize(c->own_cs);
     if (c->xs) cudaStreamSynchronize(c->xs);
-    void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_tscale, c->d_c4, c->d_c4r,
+    void *ptrs[] = {c->d_colxy, c->d_colrow, c->d_tilebox, c->d_vrows, c->d_t2, c->d_t2c, c->d_tscale, c->d_c4, c->d_c4r, c->d_c4rw,
                     c->d_h, c->d_invl2, c->d_km, c->d_kc, c->d_cnt, c->d_graw, c->d_geom, c->d_cls,
                     c->d_order, c->d_cstart, c->d_nlive, c->d_table, c->d_hdr[0], c->d_hdr[1], c->d_smp[0],
                     c->d_smp[1], c->d_raw[0], c->d_raw[1], c->d_status, c->d_hits, c->d_x, c->d_y, c->d_lgraw, c->d_lgeom,
@@ -878,7 +921,10 @@ extern "C" int kpstm_add_traces(kpstm_ctx *c, const int32_t *hdr_be, const float
     KP_CUDA(cudaEventRecord(c->copy_done[s], c->xs));
     KP_CUDA(cudaStreamWaitEvent(c->cs, c->copy_done[s], 0));
     st = run_block(c, c->d_hdr[s], c->d_smp[s], ntr);
-    if (st) return st;
+    if (st) {
+        cudaEventSynchronize(c->copy_done[s]); /* the caller's buffers are read before it hears back */
+        return st;
+    }
     KP_CUDA(cudaEventRecord(c->comp_done[s], c->cs));
     c->slot ^= 1;
     /* the caller may reuse its buffers once they have been read */
@@ -1105,6 +1151,15 @@ extern "C" int kpstm_profile_read(kpstm_ctx *c, kpstm_profile *out)
 
 /* ------------------------------------------------------------------------ */
 /* Launch configuration and autotuner (kpstm_launch). */
+
+extern "C" int kpstm_debug_wait_limit(kpstm_ctx *c, uint32_t polls)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    drop_graphs(c); /* captured launches hold the old limit */
+    c->wait_polls = polls;
+    return KPSTM_OK;
+}
 
 extern "C" int kpstm_get_launch(const kpstm_ctx *c, kpstm_launch *cfg)
 {
@@ -1362,6 +1417,7 @@ static KpImageArgs image_args(const kpstm_ctx *c)
     a.tile_r2 = r * r;
     a.aax = (float)p->iline_distance;
     a.aay = (float)p->xline_distance;
+    a.wait_polls = c->wait_polls;
     return a;
 }
 

@@ -46,6 +46,7 @@ struct KpPrepArgs {
     float *table;                  /* [nslot][row] */
     const double *c4;              /* [ns] 4*t2[t] */
     const double *c4r;             /* [ns] RN(1/(4*t2[t])) */
+    const float2 *c4rw;            /* [ns + 2] 1/(4 t2[t]) (t < ns), 1/(dt t)^2 (tail) as double-word floats */
     int64_t row;                   /* floats per table row */
     int ns, tm, full, hilo;        /* hilo: full-mode rows of float4 {hi, lo, dP, 0} */
     int exact;                     /* reference-mode taps from double integrals (precision mode) */
@@ -82,6 +83,7 @@ struct KpImageArgs {
     int *queue;                    /* persistent mode: work-item counter (zeroed per launch) */
     int nitems;                    /* persistent mode: ntile * nwin * classes */
     const int32_t *cls_order;      /* persistent mode: classes, largest first */
+    uint32_t wait_polls;           /* polls before a stage wait gives up (KP_WAIT_POLLS) */
 };
 
 /* ------------------------------------------------------------------------ */
@@ -230,9 +232,11 @@ __global__ void __launch_bounds__(1024) k_class_order(const int32_t *class_start
    D[T] = -2P[T] + P[T-2] + P[T+2] summed in double (:1391-1392), plus a zero
    sentinel D[ns].
    Full mode: the double running integral P of the unscaled trace (P = 0
-   before the trace, f = 0 after it), accumulated in double and stored over
-   [-tm, ns+tm-4] as pairs {P[i], P[i+1]-P[i]} for linear interpolation
-   (ns + 2tm - 3 entries per row). */
+   before the trace, f = 0 after it), accumulated in double-word floats and
+   stored over [-tm, ns+tm-4] as pairs {P[i], P[i+1]-P[i]} for linear
+   interpolation (ns + 2tm - 3 entries per row).  Only the reference-mode
+   branch, whose steps the reference defines in double (Kirchhoff.c:1316),
+   uses FP64. */
 __global__ void k_prep(KpPrepArgs a)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -257,42 +261,49 @@ __global__ void k_prep(KpPrepArgs a)
             if (a.hilo) q4[tm - j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             else q[tm - j] = make_float2(0.0f, 0.0f);
         }
-        double p1 = 0.0, p2 = 0.0;
+        /* P1 (running sum of the samples) and P2 (running sum of P1) as
+           double-word floats: no FP64 on the device, ~48 bits */
+        kp_dw p1 = {0.0f, 0.0f}, p2 = {0.0f, 0.0f};
         /* last P index stored: the imaging kernel reads entry floor(x) + tm with
            x = RN(x0 + Lf) <= ns - 2 + lmax (x0 < ns - 2, Lf <= lmax; the sum can
            round up onto the bound) and lmax <= tm - 1, i.e. entries
            0 .. ns + 2tm - 3 */
         const int iend = ns + tm - 3;
         for (int t = 0; t <= iend + 1; ++t) {
-            if (t < ns) p1 += (double)KP_SAMPLE(t);
-            const double prev = p2;
-            p2 += p1; /* P[t] */
+            if (t < ns) p1 = kp_dw_add1(p1, KP_SAMPLE(t));
+            const kp_dw prev = p2;
+            p2 = kp_dw_add(p2, p1); /* P[t] */
             if (a.hilo) {
-                const float hi = (float)prev;
-                q4[t - 1 + tm] = make_float4(hi, (float)(prev - (double)hi), (float)p1, 0.0f);
+                /* {hi, lo} of P[t-1]: the normalised pair is its float rounding
+                   and the remainder */
+                q4[t - 1 + tm] = make_float4(prev.h, prev.l, p1.h, 0.0f);
             } else {
-                q[t - 1 + tm] = make_float2((float)prev, (float)p1); /* entry of P index t-1 */
+                q[t - 1 + tm] = make_float2(prev.h, p1.h); /* entry of P index t-1 */
             }
         }
         return;
     }
     if (a.exact) {
-        /* the same integrals and taps, every step in double, rounded once
-           when the tap is stored (no float running sums) */
-        const double fl = (double)KP_SAMPLE(ns - 1), dtd = (double)a.dt;
-        double q1 = (double)KP_SAMPLE(0), q2 = q1;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = q2, n1 = 0.0, n2 = 0.0;
+        /* the same integrals and taps in double-word floats (no FP64 on the
+           device), rounded once when the tap is stored (no float running
+           sums); c4rw[t] = 1/(4 t2[t]) for t < ns, 1/(dt t)^2 for the two
+           tail steps, as double-word floats */
+        const float fl = KP_SAMPLE(ns - 1);
+        kp_dw q1 = {KP_SAMPLE(0), 0.0f}, q2 = q1;
+        kp_dw s0 = {0.0f, 0.0f}, s1 = s0, s2 = s0, s3 = s0, s4 = q2, n1 = s0, n2 = s0;
         for (int t = 1; t < ns + 2; ++t) {
-            if (t < ns) q1 += kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]);
-            else q1 += fl / (dtd * dtd * (double)t * (double)t);
-            q2 += q1;
+            const float2 r = a.c4rw[t];
+            q1 = kp_dw_add(q1, kp_dw_mul1(kp_dw{r.x, r.y}, t < ns ? KP_SAMPLE(t) : fl));
+            q2 = kp_dw_add(q2, q1);
             if (t == 1) n1 = q2;
             if (t == 2) n2 = q2;
             s0 = s1; s1 = s2; s2 = s3; s3 = s4; s4 = q2;
             if (t >= 2) {
                 const int T = t - 2;
-                const double pm = T >= 2 ? s0 : (T == 1 ? n1 : n2);
-                if (T < ns) row[T] = (float)(-2.0 * s2 + pm + s4);
+                const kp_dw pm = T >= 2 ? s0 : (T == 1 ? n1 : n2);
+                /* -2 s2 + pm + s4: the doubling is exact */
+                const kp_dw d = kp_dw_add(kp_dw_add(kp_dw{-2.0f * s2.h, -2.0f * s2.l}, pm), s4);
+                if (T < ns) row[T] = __fadd_rn(d.h, d.l);
             }
         }
         row[ns] = 0.0f;
@@ -543,7 +554,7 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
             const uint32_t q = nb + (uint32_t)j;
             const int slot = (int)(q % S);
             if (vflag[0]) break;
-            if (!kp_mbar_wait(&s_bar[slot], (q / S) & 1)) {
+            if (!kp_mbar_wait(&s_bar[slot], (q / S) & 1, a.wait_polls)) {
                 vflag[0] = 1;
                 kp_fail(a.status, KPSTM_ERR_TIMEOUT);
                 break;
@@ -752,7 +763,8 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     }
     if (abort) {
         /* leave no copy landing in shared memory: at most one phase per stage
-           is outstanding, the last one issued */
+           is outstanding, the last one issued; these waits keep the full
+           bound whatever a.wait_polls is */
         if (tid == 0)
             for (int sl = 0; sl < S; ++sl)
                 if (s_last[sl] >= 0) kp_mbar_wait(&s_bar[sl], ((uint32_t)s_last[sl] / S) & 1);

@@ -28,3 +28,14 @@ def rel_l2(a, b) -> float:
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def config1_golden() -> dict:
+    """The compiled reference's full config-1 image as recorded by
+    tests/golden/make_golden.py (SHA-256 of its float32 bytes and norms)."""
+    return json.loads((GOLDEN / "config1_full.json").read_text())
+
+
+def image_sha256(img) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(img, dtype="<f4").tobytes()).hexdigest()

@@ -14,11 +14,17 @@ Stored per fixture (``<name>.npz``):
     su_headers    [ntraces, 60] int32: the SU header words it wrote
     jobs          (jobs_x, jobs_y)
 
+Also ``config1_full.json``: the reference's image of the full config-1
+line (synth.line2d(): 200 CMPs x 48 offsets, 1001 samples, 1.61e9 pairs,
+one rank), too large to store, recorded as the SHA-256 of its float32
+bytes ([traces][ns], little-endian, SU trace order) with its norm.
+
 Run here (needs the reference checkout and gcc):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import sys
 import tempfile
@@ -61,7 +67,21 @@ def run_reference(s, jx: int, jy: int, work: Path):
     return refbuild.read_image(work / "run", s.ns, jx * jy)
 
 
+def config1_full() -> dict:
+    s = synth.line2d()
+    with tempfile.TemporaryDirectory() as td:
+        _, img = run_reference(s, 1, 1, Path(td))
+    img = np.ascontiguousarray(img, dtype="<f4")
+    return {"survey": "synth.line2d()", "traces": int(img.shape[0]), "ns": int(img.shape[1]),
+            "jobs": [1, 1], "reference": "Kirchhoff.c via oracle/refbuild.py, -O0 -w -ffast-math, one rank",
+            "sha256": hashlib.sha256(img.tobytes()).hexdigest(),
+            "l2_norm": float(np.linalg.norm(img.astype(np.float64))),
+            "max_abs": float(np.max(np.abs(img)))}
+
+
 def main():
+    (HERE / "config1_full.json").write_text(json.dumps(config1_full(), indent=1) + "\n")
+    print("config1_full.json")
     for name, (s, jx, jy) in fixtures().items():
         with tempfile.TemporaryDirectory() as td:
             hdr, img = run_reference(s, jx, jy, Path(td))

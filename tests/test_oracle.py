@@ -84,3 +84,18 @@ def test_oracle_matches_fresh_reference_runs(oracle_lib, seed):
         _, ref = refbuild.read_image(td / "run", ns, jx * jy)
     got = _oracle_job_images(oracle_lib, s, jx, jy)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), rel_l2(got, ref)
+
+
+def test_restatement_is_the_reference_on_config1_full(oracle_lib):
+    """Config 1 at full size (200 CMPs x 48 offsets x 1001 samples, 1.61e9
+    pairs): the C restatement's finished image has exactly the bytes of the
+    compiled reference's own output (its SHA-256 recorded by
+    tests/golden/make_golden.py)."""
+    from fixtures import config1_golden, image_sha256
+    gold = config1_golden()
+    s = synth.line2d()
+    o = oracle_lib.kirchhoff(s, want_acc=False)
+    img = o["image"].reshape(-1, s.ns)
+    assert img.shape == (gold["traces"], gold["ns"])
+    assert image_sha256(img) == gold["sha256"]
+    assert o["pairs"] > 1.5e9
