@@ -292,8 +292,11 @@ int kpstm_lsm_pair_count(kpstm_ctx *ctx, int64_t *pairs);
 
 /* ---- finishing without device allocation ------------------------------------ */
 
-/* Largest image (nx*ny*nh*ns samples) kpstm_finish_noalloc accepts. */
+/* Largest image (nx*ny*nh*ns samples) and largest ns kpstm_finish_noalloc
+   accepts (ns: the low-pass convolution keeps 10 ns floats in one CTA's
+   shared memory). */
 #define KPSTM_NOALLOC_MAX_SAMPLES 4194304
+#define KPSTM_NOALLOC_MAX_NS 5600
 
 /* The finishing step of kpstm_finish for callers that must not allocate
    device memory.  No counterpart in the reference (it has no device).
@@ -308,11 +311,16 @@ int kpstm_lsm_pair_count(kpstm_ctx *ctx, int64_t *pairs);
    low-pass impulse response live in one fixed array compiled into the
    library - about 17 MB that every GPU which loads the library holds until
    the process exits.  Images larger than KPSTM_NOALLOC_MAX_SAMPLES samples
-   are refused with KPSTM_ERR_TOO_LARGE; params are checked as in
-   kpstm_create (no context is needed).
+   or with more than KPSTM_NOALLOC_MAX_NS samples per trace are refused with
+   KPSTM_ERR_TOO_LARGE; params are checked as in kpstm_create (no context is
+   needed).
 
    The first call on a device looks up that array's device address (with
    the device current); make that first call before any stream capture.
+   The address is kept for the life of the process and does not survive
+   cudaDeviceReset.  The low-pass response is computed on the host and
+   copied into the array (from a static host buffer) when ns, dt or the
+   cutoff differ from the previous call on the device.
    Work is queued on cuda_stream (NULL: the default stream) and the call
    returns without waiting; synchronise before reading d_out.  All calls on
    a device share the one array, so calls whose work overlaps on the GPU

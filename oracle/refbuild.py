@@ -39,7 +39,9 @@ HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 SHIM_DIR = HERE / "shim"
 PATCHED = REF_DIR / "Kirchhoff_kref.c"
-REFERENCE_SOURCE = Path(os.environ.get("KPSTM_REFERENCE_DIR", "/root/reference")) / "Kirchhoff.c"
+# the reference checkout: KPSTM_REFERENCE_DIR, else a "reference" directory
+# beside this repository
+REFERENCE_SOURCE = Path(os.environ.get("KPSTM_REFERENCE_DIR", HERE.parent.parent / "reference")) / "Kirchhoff.c"
 
 # Numeric configuration macros of Kirchhoff.c:17-65, in file order.
 NUMERIC = [

@@ -1,7 +1,7 @@
 """ctypes binding of the C ABI declared in include/kpstm.h.
 
 This is the binding a Python caller of the reference's kirchhoff() job would
-add (see INTEGRATION.md): the structures mirror kpstm_params /
+add: the structures mirror kpstm_params /
 kpstm_velocity / kpstm_dims field for field, and ``load()`` opens the
 in-tree ``libkpstm.so`` built by ``random_gb300.build``.  There is no
 fallback: if the library is missing or no GPU is visible the calls fail.
@@ -28,6 +28,7 @@ STATUS = {
     11: "KPSTM_ERR_UNSUPPORTED", 12: "KPSTM_ERR_TRANGE", 13: "KPSTM_ERR_TOO_LARGE",
 }
 NOALLOC_MAX_SAMPLES = 4194304
+NOALLOC_MAX_NS = 5600
 
 # kpstm_cg_monitor: int (*)(int32_t iteration, const float *d_model, double resid_k, void *user)
 CG_MONITOR = C.CFUNCTYPE(C.c_int, C.c_int32, C.c_void_p, C.c_double, C.c_void_p)

@@ -1283,59 +1283,69 @@ extern "C" int kpstm_autotune(kpstm_ctx *c, const int32_t *d_hdr_be, const float
    k_deriv and k_lowpass, and the low-pass impulse response - is this one
    file-scope array instead of context buffers.  Nothing in it has to start
    at zero: every call rewrites the parts it reads. */
-#define KP_NOALLOC_MAX_NS 32768
-static __device__ __align__(256) float g_noalloc_scratch[KPSTM_NOALLOC_MAX_SAMPLES + KP_NOALLOC_MAX_NS];
+/* ns is bounded by k_lowpass's shared memory (2 ns + 8 ns floats <= 220 KB) */
+static_assert(sizeof(float) * (((2 * KPSTM_NOALLOC_MAX_NS + 3) & ~3) + KPSTM_NOALLOC_MAX_NS * KP_LP_ROWS) <= 220 * 1024,
+              "KPSTM_NOALLOC_MAX_NS exceeds the low-pass kernel's shared memory");
+static __device__ __align__(256) float g_noalloc_scratch[KPSTM_NOALLOC_MAX_SAMPLES + KPSTM_NOALLOC_MAX_NS];
 
 /* Device address of g_noalloc_scratch per device, looked up once per device
    with that device current (the array's name is only a host-side handle in
-   host code). */
+   host code), and the low-pass response last uploaded there: (ns, dt,
+   cutoff) of the last upload, so that calls with the same sampling and
+   filter skip it.  The cache does not survive cudaDeviceReset. */
 #define KP_NOALLOC_MAX_DEVICES 64
 static float *g_noalloc_ptr[KP_NOALLOC_MAX_DEVICES];
+struct kp_noalloc_key {
+    int ns;
+    float dt;
+    double cutoff;
+};
+static kp_noalloc_key g_noalloc_key[KP_NOALLOC_MAX_DEVICES];
+static double g_noalloc_hd[KPSTM_NOALLOC_MAX_NS]; /* host staging of the response (no allocation) */
+static float g_noalloc_hf[KPSTM_NOALLOC_MAX_NS];
 static pthread_mutex_t g_noalloc_mu = PTHREAD_MUTEX_INITIALIZER;
 
-static int noalloc_scratch(float **out)
+/* The scratch of this device, with the low-pass impulse response of params
+   (kpstm_lowpass_kernel, the host computation kpstm_finish uses) in its last
+   KPSTM_NOALLOC_MAX_NS floats. */
+static int noalloc_scratch(const kpstm_params *params, cudaStream_t stream, float **out)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return KPSTM_ERR_NO_DEVICE;
     if (dev < 0 || dev >= KP_NOALLOC_MAX_DEVICES) return KPSTM_ERR_UNSUPPORTED;
+    int st = KPSTM_OK;
     pthread_mutex_lock(&g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            pthread_mutex_unlock(&g_noalloc_mu);
-            return KPSTM_ERR_CUDA;
+    do {
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                st = KPSTM_ERR_CUDA;
+                break;
+            }
+            g_noalloc_ptr[dev] = (float *)p;
         }
-        g_noalloc_ptr[dev] = (float *)p;
-    }
-    *out = g_noalloc_ptr[dev];
+        kp_noalloc_key &k = g_noalloc_key[dev];
+        if (k.ns != params->ns || k.dt != params->dt || k.cutoff != params->anti_alias_cutoff) {
+            const int ns = params->ns;
+            if ((st = kpstm_lowpass_kernel(params, g_noalloc_hd))) break;
+            for (int i = 0; i < ns; ++i) g_noalloc_hf[i] = (float)g_noalloc_hd[i];
+            /* from pageable memory: returns once the bytes are staged, so the
+               host buffer may be reused */
+            if (cudaMemcpyAsync(g_noalloc_ptr[dev] + KPSTM_NOALLOC_MAX_SAMPLES, g_noalloc_hf, sizeof(float) * ns,
+                                cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+                k.ns = 0;
+                st = KPSTM_ERR_CUDA;
+                break;
+            }
+            k.ns = ns;
+            k.dt = params->dt;
+            k.cutoff = params->anti_alias_cutoff;
+        }
+        *out = g_noalloc_ptr[dev];
+    } while (0);
     pthread_mutex_unlock(&g_noalloc_mu);
-    return KPSTM_OK;
-}
-
-/* Low-pass impulse response h[m] = (1/ns) sum_k A[k] cos(2 pi k m / ns), with
-   the anti-alias spectrum A of Kirchhoff.c:380-441 evaluated per bin in the
-   same float/double steps as kpstm_aliasfilter (fs, den from the host). */
-__global__ void k_noalloc_impulse(int ns, float fs, float den, float *h)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= ns) return;
-    const int half = ns / 2;
-    double acc = 0.0;
-    for (int k = 0; k < ns; ++k) {
-        int j = k;
-        bool zero = (ns & 1) && (k == half || k == half + 1);
-        if (k > half) j = ns - k;
-        float a = 0.0f;
-        if (!zero) {
-            float x = __fmul_rn(__int2float_rn(j), fs);
-            float num = __fmul_rn(__fmul_rn(__fmul_rn(x, x), x), x);
-            a = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, (double)__fdiv_rn(num, den)))));
-        }
-        long long km = ((long long)k * m) % ns;
-        acc += (double)a * cos(6.283185307179586476925286766559 * (double)km / (double)ns);
-    }
-    h[m] = (float)(acc / ns);
+    return st;
 }
 
 /* k_deriv for accumulators in the caller's layout [col][cls][ns] with the
@@ -1361,21 +1371,13 @@ extern "C" int kpstm_finish_noalloc(const kpstm_params *params, const float *d_k
     if (st) return st;
     const int ns = params->ns;
     const int64_t n = s.dims.out_elems;
-    if (n > KPSTM_NOALLOC_MAX_SAMPLES || ns > KP_NOALLOC_MAX_NS) return KPSTM_ERR_TOO_LARGE;
+    if (n > KPSTM_NOALLOC_MAX_SAMPLES || ns > KPSTM_NOALLOC_MAX_NS) return KPSTM_ERR_TOO_LARGE;
     const size_t smem = sizeof(float) * (((2 * (size_t)ns + 3) & ~size_t(3)) + (size_t)ns * KP_LP_ROWS);
-    if (smem > 220 * 1024) return KPSTM_ERR_TOO_LARGE;
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
     float *scratch = nullptr;
-    st = noalloc_scratch(&scratch);
+    st = noalloc_scratch(params, stream, &scratch);
     if (st) return st;
     float *x = scratch, *h = scratch + KPSTM_NOALLOC_MAX_SAMPLES;
-    /* scalars of create_aliasfilter (Kirchhoff.c:403-412), as kpstm_aliasfilter */
-    const float fs = (float)(2.0 / ((double)params->dt * (double)ns));
-    float fm = (float)params->anti_alias_cutoff;
-    fm = (float)((double)fm * 3.0);
-    const float den = ((fm * fm) * fm) * fm;
-    cudaStream_t stream = (cudaStream_t)cuda_stream;
-    k_noalloc_impulse<<<(ns + 127) / 128, 128, 0, stream>>>(ns, fs, den, h);
-    KP_CUDA(cudaGetLastError());
     k_deriv_caller<<<1024, 256, 0, stream>>>(d_km, d_fold, n, ns, params->dt, x);
     KP_CUDA(cudaGetLastError());
     KP_CUDA(cudaFuncSetAttribute(k_lowpass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -53,7 +53,7 @@ const char *kpstm_strerror(int st)
     case KPSTM_ERR_SEGY: return "malformed SEG-Y data";
     case KPSTM_ERR_UNSUPPORTED: return "not supported by this build";
     case KPSTM_ERR_TRANGE: return "trangeMax < 2: triangle taps would leave the trace";
-    case KPSTM_ERR_TOO_LARGE: return "image larger than the fixed scratch of kpstm_finish_noalloc";
+    case KPSTM_ERR_TOO_LARGE: return "image or trace length beyond the fixed scratch of kpstm_finish_noalloc";
     default: return "unknown status";
     }
 }

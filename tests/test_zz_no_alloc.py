@@ -78,3 +78,33 @@ def test_noalloc_finish_refuses_images_beyond_its_scratch(kpstm_lib):
     st = kpstm_lib.kpstm_finish_noalloc(C.byref(prm), d.data_ptr(), d.data_ptr(), d.data_ptr(), None)
     assert st == 13  # KPSTM_ERR_TOO_LARGE
     assert b"noalloc" in kpstm_lib.kpstm_strerror(13)
+
+
+def test_noalloc_finish_full_mode_offset_classes(kpstm_lib):
+    """Full physics on the rotated 3-D patch with 4 offset classes: the
+    accumulators arrive scaled by t/(8 dt) per sample, as
+    kpstm_get_accumulators returns them, and finish like kpstm_finish."""
+    torch = pytest.importorskip("torch")
+    p, km, fold, image = _accumulators("g3_patch_rotated", mode=capi.MODE_FULL)
+    assert km.shape[2] == 4
+    d_km, d_fold = torch.from_numpy(km).cuda(), torch.from_numpy(fold).cuda()
+    prm = capi.make_params(p)
+    for _ in range(2):
+        d_out = torch.full(km.shape, float("nan"), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        assert kpstm_lib.kpstm_finish_noalloc(C.byref(prm), d_km.data_ptr(), d_fold.data_ptr(),
+                                              d_out.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        assert rel_l2(d_out.cpu().numpy(), image) <= TOL
+
+
+def test_noalloc_finish_refuses_long_traces(kpstm_lib):
+    """ns beyond KPSTM_NOALLOC_MAX_NS (the low-pass kernel's shared memory) is
+    refused even for a one-column image."""
+    torch = pytest.importorskip("torch")
+    s, *_ = load("g1_line_oddns")
+    p = dict(s.params, ns=capi.NOALLOC_MAX_NS + 1, end_iline=s.params["start_iline"] + 1, nh=1)
+    d = torch.zeros(8, dtype=torch.float32, device="cuda")  # never touched
+    prm = capi.make_params(p)
+    st = kpstm_lib.kpstm_finish_noalloc(C.byref(prm), d.data_ptr(), d.data_ptr(), d.data_ptr(), None)
+    assert st == 13  # KPSTM_ERR_TOO_LARGE
