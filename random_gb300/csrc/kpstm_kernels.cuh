@@ -642,10 +642,6 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                            ~1e-14 for noisy traces (least-squares operators) */
                         const float2 *q2 = reinterpret_cast<const float2 *>(tab) + (a.tm - 1);
                         const float4 *q4 = reinterpret_cast<const float4 *>(tab) + (a.tm - 1);
-                        /* shared-window addresses with the floor's magic bits folded in:
-                           entry b - KP_MAGIC_BITS is at qa2 + 8 b (mod 2^32) */
-                        const uint32_t qa2 = kp_smem(q2) - (uint32_t)KP_MAGIC_BITS * 8u;
-                        const uint32_t qa4 = kp_smem(q4) - (uint32_t)KP_MAGIC_BITS * 16u;
                         const float4 *sv4 = reinterpret_cast<const float4 *>(s_v) + w * (K / 2) * 32 + lane;
                         /* the triangle-filtered tap of one sample from the floors' bits
                            b* and the fractions f* of y = Tf, Tf + Lf, Tf - Lf; second
@@ -655,13 +651,13 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                         auto tri_of = [&](int b0, int ba, int bb, float m2f0, float fa, float fb) -> float {
                             /* m2f0 = -2 f0 */
                             if (HILO) {
-                                const float4 Q0 = kp_lds4(qa4 + 16u * (uint32_t)b0), Qa = kp_lds4(qa4 + 16u * (uint32_t)ba);
-                                const float4 Qb = kp_lds4(qa4 + 16u * (uint32_t)bb);
+                                const float4 Q0 = q4[b0 - KP_MAGIC_BITS], Qa = q4[ba - KP_MAGIC_BITS];
+                                const float4 Qb = q4[bb - KP_MAGIC_BITS];
                                 const float big = ((Qa.x - Q0.x) + (Qb.x - Q0.x)) + ((Qa.y - Q0.y) + (Qb.y - Q0.y));
                                 return fmaf(m2f0, Q0.z, fmaf(fa, Qa.z, fmaf(fb, Qb.z, big)));
                             } else {
-                                const float2 Q0 = kp_lds2(qa2 + 8u * (uint32_t)b0), Qa = kp_lds2(qa2 + 8u * (uint32_t)ba);
-                                const float2 Qb = kp_lds2(qa2 + 8u * (uint32_t)bb);
+                                const float2 Q0 = q2[b0 - KP_MAGIC_BITS], Qa = q2[ba - KP_MAGIC_BITS];
+                                const float2 Qb = q2[bb - KP_MAGIC_BITS];
                                 /* each interpolation term joins the table difference of its
                                    own tap (values of like size), the centre term last */
                                 const float ua = fmaf(fa, Qa.y, Qa.x - Q0.x), ub = fmaf(fb, Qb.y, Qb.x - Q0.x);
