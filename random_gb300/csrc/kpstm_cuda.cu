@@ -1565,8 +1565,10 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     }
     a.rvdt = c->d_rvdt;
     a.acc = use_sh ? nullptr : c->d_dacc;
-    void (*dm)(KpDemigArgs) = use_sh ? k_demig<true> : k_demig<false>;
+    void (*dm)(KpDemigArgs) = use_sh ? k_demig<true, false> : k_demig<false, false>;
+    void (*dmb)(KpDemigArgs) = use_sh ? k_demig<true, true> : k_demig<false, true>;
     KP_CUDA(cudaFuncSetAttribute(dm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KP_CUDA(cudaFuncSetAttribute(dmb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned nblk = (unsigned)((c->lsm_nlive + KP_DM_WARPS - 1) / KP_DM_WARPS);
     if (!c->dbound_ok) {
         /* once per geometry: max_k (L 1)[trace, k], the fixed-point range of each trace */
@@ -1575,7 +1577,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
         b.dbound_out = c->d_dbound;
         b.wbound_out = c->d_wbound;
         if (!use_sh) KP_CUDA(cudaMemsetAsync(c->d_dacc, 0, accb, c->cs));
-        dm<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
+        dmb<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(b);
         KP_CUDA(cudaGetLastError());
         c->dbound_ok = 1;
     }

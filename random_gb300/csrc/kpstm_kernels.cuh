@@ -964,8 +964,10 @@ __host__ __device__ inline size_t kp_demig_smem(int ns, int ng, bool sh)
    of entries, the low and high words of each value stored back in the two
    limbs).
    Else (long rows) the entries are added with fire-and-forget 64-bit RED
-   into the trace's row in global memory, which stays in L2. */
-template <bool SH>
+   into the trace's row in global memory, which stays in L2.
+   BOUND: the bound pass (compiled apart, so that the main pass carries none
+   of its per-sample work). */
+template <bool SH, bool BOUND>
 __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigArgs a)
 {
     extern __shared__ __align__(16) float dm_smem[];
@@ -983,7 +985,7 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
     if (SH)
         for (int i = lane; i < 2 * ngp; i += 32) s_lo[i] = 0;
     __syncthreads();
-    const bool bound = a.model == nullptr;
+    constexpr bool bound = BOUND; /* the bound pass: the all-ones model (a.model unused) */
     const unsigned int mb = bound ? __float_as_uint(1.0f) : *a.absmax;
     if (mb == 0u) return; /* zero model: the data stay zero */
     if (mb >= 0x7f800000u) {
