@@ -924,32 +924,6 @@ __device__ __forceinline__ void kp_split(float x, float sR, float nR, int &h, in
     l = __float_as_int(__fadd_rn(lf, KP_MAGIC)) - KP_MAGIC_BITS;
 }
 
-/* One tap of the transpose for the 32 lanes of a warp: e0 (limbs l0, h0) at
-   entry n and e1 (l1, h1) at n + 1 of the warp's limb rows; entries below 0
-   are dropped, n = KP_DM_NONE marks a lane without a pair.  Where the
-   operator's traveltime is flat in t, many of the warp's consecutive samples
-   land on the same entry and their shared atomics would serialise; so the
-   lanes are grouped by entry (match), each group's limbs are summed
-   (reduce), and one lane per group issues the atomics.  The sums are the
-   same integers, so the limb bounds and the result are unchanged.  All
-   lanes must call it. */
-__device__ __forceinline__ void kp_demig_tap(int *lo, int *hi, int n, int l0, int h0, int l1, int h1, int lane)
-{
-    const unsigned g = __match_any_sync(0xffffffffu, n);
-    const int s0l = __reduce_add_sync(g, l0), s0h = __reduce_add_sync(g, h0);
-    const int s1l = __reduce_add_sync(g, l1), s1h = __reduce_add_sync(g, h1);
-    if (lane == __ffs(g) - 1) {
-        if (n >= 0) {
-            atomicAdd(lo + n, s0l);
-            atomicAdd(hi + n, s0h);
-        }
-        if (n >= -1) {
-            atomicAdd(lo + n + 1, s1l);
-            atomicAdd(hi + n + 1, s1h);
-        }
-    }
-}
-
 /* Dynamic shared memory of k_demig: t2[ns] and ts[ns], then (SH) one
    accumulator row per warp: ngp int32 low limbs followed by ngp int32 high
    limbs (ngp = ng rounded up to a multiple of 4). */
@@ -1134,11 +1108,32 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
                         kp_split(gs, sR, nR, qh, ql);
                         /* tap at ya (c = 1): e1 = RN(gs fa) at na + 1, e0 = Q - e1 at na */
                         kp_split(__fmul_rn(gs, fa), sR, nR, h1, l1);
-                        kp_demig_tap(s_lo, s_hi, ok ? na : KP_DM_NONE, ql - l1, qh - h1, l1, h1, lane);
+                        if (ok && na >= 0) {
+                            atomicAdd(s_lo + na, ql - l1);
+                            atomicAdd(s_hi + na, qh - h1);
+                        }
+                        if (ok && na >= -1) {
+                            atomicAdd(s_lo + na + 1, l1);
+                            atomicAdd(s_hi + na + 1, h1);
+                        }
                         kp_split(__fmul_rn(gs, fb), sR, nR, h1, l1); /* tap at yb (c = 1) */
-                        kp_demig_tap(s_lo, s_hi, ok ? nb : KP_DM_NONE, ql - l1, qh - h1, l1, h1, lane);
+                        if (ok && nb >= 0) {
+                            atomicAdd(s_lo + nb, ql - l1);
+                            atomicAdd(s_hi + nb, qh - h1);
+                        }
+                        if (ok && nb >= -1) {
+                            atomicAdd(s_lo + nb + 1, l1);
+                            atomicAdd(s_hi + nb + 1, h1);
+                        }
                         kp_split(__fmul_rn(-2.0f * gs, f0), sR, nR, h1, l1); /* tap at y0 (c = -2) */
-                        kp_demig_tap(s_lo, s_hi, ok ? n0 : KP_DM_NONE, -2 * ql - l1, -2 * qh - h1, l1, h1, lane);
+                        if (ok && n0 >= 0) {
+                            atomicAdd(s_lo + n0, -2 * ql - l1);
+                            atomicAdd(s_hi + n0, -2 * qh - h1);
+                        }
+                        if (ok && n0 >= -1) {
+                            atomicAdd(s_lo + n0 + 1, l1);
+                            atomicAdd(s_hi + n0 + 1, h1);
+                        }
                     } else {
                         const long long Q = kp_f2ll_rn45(gs);
                         const long long a1 = kp_f2ll_rn45(__fmul_rn(gs, fa));
