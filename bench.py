@@ -359,6 +359,33 @@ def run_ours(args, rank, world, local_rank):
     del fold
     del m
 
+    # -------- the reference's own operator (nearest-sample traveltime, fixed
+    # triangle, unit weight: the mode that reproduces Kirchhoff.c bit for bit)
+    # on the same survey and blocks, so that the CPU baseline, which runs that
+    # operator, has a same-operator GPU figure beside the full-physics headline
+    same_op = None
+    if not args.no_cpu:
+        mr = Migration(dict(prm, mode=capi.MODE_REFERENCE), s.velocity)
+        mr.set_stream(stream.cuda_stream)
+        for i in range(2):
+            step_m = (i % nblocks) * block
+            mr.add_traces_device(d_hdr.data_ptr() + step_m * 240, d_smp.data_ptr() + step_m * row_bytes, block)
+        mr.synchronize()
+        pr0 = mr.pairs()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        nref = min(args.steps, 3)
+        for i in range(nref):
+            step_m = ((2 + i) % nblocks) * block
+            mr.add_traces_device(d_hdr.data_ptr() + step_m * 240, d_smp.data_ptr() + step_m * row_bytes, block)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        same_op = {"gpu_reference_mode_gpairs_s": round((mr.pairs() - pr0) / (r0.elapsed_time(r1) / 1e3) / 1e9, 4),
+                   "steps": nref, "launch": mr.launch_config(),
+                   "note": "the reference operator on the GPU (accumulators bit for bit equal to Kirchhoff.c's), "
+                           "same survey and blocks as the headline"}
+        del mr
+
     # -------- e2e through the C ABI from pinned host memory
     e2e = None
     if not args.no_e2e:
@@ -397,6 +424,8 @@ def run_ours(args, rank, world, local_rank):
                          f"400 one-iline slabs, first {args.cpu_traces} traces of the survey, one rank per "
                          f"core: {pairs_c} pairs in {secs_c:.2f} s"}
 
+    if same_op and cpu:
+        same_op["ratio_to_cpu_baseline"] = round(same_op["gpu_reference_mode_gpairs_s"] / cpu["value"], 1)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
@@ -413,6 +442,7 @@ def run_ours(args, rank, world, local_rank):
             "pairs": int(pairs_all), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "profile_ms": {"image": round(prof["image_ms"], 3), "prep": round(prof["prep_ms"], 3)},
             "live_pair_fraction": round(live_fraction, 4),
+            "same_operator": same_op,
             "trace_storage": {"bytes_per_trace": NS * (2 if args.precision == "bf16" else 4) +
                               (4 if args.precision == "bf16" else 0),
                               "gb_per_s": round(block * (NS * (2 if args.precision == "bf16" else 4)) /
