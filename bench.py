@@ -164,7 +164,7 @@ def profile_constants(name: str) -> dict | None:
 
 
 def imaging_roofline(pairs_per_launch, t_launch, b_alg, clk, peaks, dev, launch_cfg, flavour,
-                     table_rows=None, row_bytes=None) -> dict:
+                     table_rows=None, row_bytes=None, image_columns=None) -> dict:
     """Roofline of one imaging launch.  The binding resource is the FP32
     lane-issue rate for the algorithmic op count (no tensor work; the kernel
     moves ~1e-3 byte per pair): achieved = ops/pair x pairs/s, peak = SMs x
@@ -207,10 +207,15 @@ def imaging_roofline(pairs_per_launch, t_launch, b_alg, clk, peaks, dev, launch_
                      "ncu_lts_throughput": pc.get("lts_throughput")}
     if pc.get("dram_bytes") is not None:
         # fixed part (accumulators, velocity) + table part growing with the rows staged
-        extra = 0
+        # fixed part (accumulators, velocity rows) scaled by the image columns,
+        # table part by the rows staged
+        fixed, tab = pc["dram_bytes"], 0
         if table_rows and pc.get("table_rows") and row_bytes:
-            extra = (table_rows - pc["table_rows"]) * row_bytes
-        out["traffic"] = round(pc["dram_bytes"] + extra)
+            fixed -= pc["table_rows"] * row_bytes
+            tab = table_rows * row_bytes
+        if image_columns and pc.get("image_columns"):
+            fixed *= image_columns / pc["image_columns"]
+        out["traffic"] = round(fixed + tab)
         out["traffic_source"] = (f"ncu dram bytes of the capture in profiles/{PROFILE_OF[flavour]} "
                                  f"({pc.get('case', '')}), table part scaled to this launch")
     out["profile"] = {"file": f"profiles/{PROFILE_OF[flavour]}", "kernel": pc.get("kernel"),
@@ -349,7 +354,7 @@ def run_ours(args, rank, world, local_rank):
     b_alg = algorithmic_bytes_per_step(model, block, row_floats)
     roofline = imaging_roofline(pairs / launches, t_launch, b_alg, clk, peaks, dev, launch_cfg,
                                 "full_bf16" if args.precision == "bf16" else "full",
-                                table_rows=block, row_bytes=row_floats * 4)
+                                table_rows=block, row_bytes=row_floats * 4, image_columns=args.image * args.image)
     roofline["image_kernel_share"] = round(prof["image_ms"] / (prof["image_ms"] + prof["prep_ms"]), 4)
     # live pairs: those whose traveltime falls inside the trace (the fold
     # counts), against all counted (trace, column, sample) pairs so far
@@ -554,9 +559,10 @@ def cpu_line(nprocs: int, opt: str = "-O3"):
 def run_line(args):
     """Config 1, the 2-D line: 200 CMPs x 48 offsets = 9,600 traces, 1001
     samples at 4 ms, 48 offset classes x 200 columns, reference operator
-    (accumulators bit-exact to the reference).  The launch configuration is
-    chosen by kpstm_autotune on the line itself (a fresh context), as a job
-    loop would on its first block.  A step images the whole line once
+    (accumulators bit-exact to the reference).  The launch is the one
+    kpstm_autotune picks on the line (8 x 1 tiles, K = 8, 3 CTAs per SM; with
+    --autotune N > 0 the autotuner runs on the line itself, as a job loop
+    would on its first block).  A step images the whole line once
     (1.61e9 pairs) from device-resident traces.  e2e: the same job through
     kpstm_add_traces from pinned host buffers and kpstm_finish (image and
     fold to host) per step.  CPU: the compiled reference on one rank over
@@ -575,8 +581,8 @@ def run_line(args):
     m = Migration(s.params, s.velocity)
     stream = torch.cuda.Stream(device=dev)
     m.set_stream(stream.cuda_stream)
-    if args.autotune == 0:
-        # the autotuner's choice on this line: 8 x 1 tiles, K = 8, 3 CTAs per SM, grid launch
+    if args.autotune <= 0:
+        # the autotuner's usual choice on this line: 8 x 1 tiles, K = 8, 3 CTAs per SM, grid launch
         m.set_launch(tile_px=8, samples_per_lane=8, persistent=0, ctas_per_sm=3)
         cfg, tune_ms = m.launch_config(), 0.0
     else:
@@ -1013,7 +1019,7 @@ def main():
                     help="lsm workload: finite-difference checks of the misfit gradient (random directions)")
     ap.add_argument("--autotune", type=int, default=-1,
                     help="survey workload: autotune the launch on this many traces before timing (<= 0: default "
-                         "launch); line workload: 0 uses the launch the autotuner picks there, else it autotunes")
+                         "launch); line workload: > 0 autotunes on the line, else the launch the autotuner picks there")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32",
                     help="trace storage of the survey workload (bf16: per-trace scale, Kahan sums)")
     ap.add_argument("--workload", choices=["survey", "offset-bins", "lsm", "line"], default="survey",
