@@ -525,7 +525,7 @@ def run_offset_bins(args):
 
 
 def cpu_line(nprocs: int, opt: str = "-O3"):
-    """The reference's kirchhoff() on the full config-1 line: the compiled
+    """The reference's kirchhoff() on the whole 2-D line (9,600 traces): the compiled
     Kirchhoff.c (MPI/FFTW stand-ins) with its image cut into nprocs slabs
     along the line (number_mpi_jobsX = nprocs, Kirchhoff.c:280-300), one
     process per slab, all started together; every slab reads all traces
@@ -671,7 +671,7 @@ def run_line(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(elapsed / args.steps * 1e3, 3), "higher_is_better": True, "dtype": "f32",
             "data": "synthetic (seeded 2-D line: 20 point scatterers, 25 Hz Ricker, 20 dB noise)",
-            "config": {"workload": "config 1: 2-D line, 200 CMPs x 48 offsets = 9,600 traces x 1001 samples "
+            "config": {"workload": "2-D line, 200 CMPs x 48 offsets = 9,600 traces x 1001 samples "
                                    "@ 4 ms, 200 x 48 x 1001 offset gathers, aperture 1500 m, reference operator",
                        "traces": int(s.ntr), "launch": cfg, "autotune_ms": round(tune_ms, 3),
                        "l2": "flushed between timed steps (512 MB write); each step timed alone"},
@@ -704,7 +704,7 @@ LSM_SNR_DB = 10.0
 
 def lsm_cpu_subproblem(args, dev, stream):
     """The FP64-oracle leg of the least-squares workload (bench's CPU
-    baseline for it): a 16 x 16-column crop of config 5's model with 1,000
+    baseline for it): a 16 x 16-column crop of the 200 x 200 x 751 model with 1,000
     traces of the same acquisition statistics and 4 scatterers (the full
     survey's scatterer density), d = L m_true (FP64 oracle) + 10 dB noise,
     rounded to float32 for every solver.  The oracle's FP64 CGLS (timed on
@@ -737,7 +737,7 @@ def lsm_cpu_subproblem(args, dev, stream):
             out[name] = [float(np.linalg.norm(a.astype(np.float64).reshape(b.shape) - b) / np.linalg.norm(b))
                          for a, b in zip(snaps, x64)]
     pairs = 2 * niter * 1000 * 16 * 16 * 751  # upper bound: every (trace, column, sample) of the crop
-    return {"problem": "16 x 16 columns of config 5's model (25 m, 751 x 4 ms), 1,000 traces (offsets "
+    return {"problem": "16 x 16 columns of the 200 x 200 x 751 model (25 m, 4 ms), 1,000 traces (offsets "
                        "U(0, 3000 m), random azimuths, midpoints over the crop), 12 dipping reflectors + 4 "
                        "scatterers, d = L m_true (FP64) + 10 dB noise, float32 data",
             "rel_l2_vs_fp64": {k: [round(e, 8) for e in v] for k, v in out.items()},
@@ -747,7 +747,7 @@ def lsm_cpu_subproblem(args, dev, stream):
 
 
 def run_lsm(args):
-    """Least-squares Kirchhoff migration, config 5: a 200 x 200 x 751
+    """Least-squares Kirchhoff migration: a 200 x 200 x 751
     reflectivity model (25 m, 4 ms; 12 dipping reflectors + 100 scatterers),
     d = L m_true on 250,000 traces (offsets U(0, 3000 m), random azimuths,
     751 samples) plus 10 dB Gaussian noise, aperture 3000 m, full physics;
@@ -827,7 +827,7 @@ def run_lsm(args):
             "unit": "migrations", "higher_is_better": False,
             "dtype": "bf16 data/residual store, f32 compute, f64 CG scalars",
             "data": "synthetic: d = L m_true + 10 dB Gaussian noise (seeded)",
-            "config": {"workload": "config 5: 200x200x751 reflectivity (25 m, 4 ms), 12 dipping reflectors + 100 "
+            "config": {"workload": "least-squares survey: 200x200x751 reflectivity (25 m, 4 ms), 12 dipping reflectors + 100 "
                                    "scatterers, 250,000 traces x 751 samples, offsets U(0, 3000 m), random "
                                    "azimuths, aperture 3000 m, full physics", "traces": ntr,
                        "cg_iterations": args.cg_iters},

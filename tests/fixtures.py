@@ -30,10 +30,10 @@ def rel_l2(a, b) -> float:
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def config1_golden() -> dict:
-    """The compiled reference's full config-1 image as recorded by
+def line2d_golden() -> dict:
+    """The compiled reference's full 2-D line image as recorded by
     tests/golden/make_golden.py (SHA-256 of its float32 bytes and norms)."""
-    return json.loads((GOLDEN / "config1_full.json").read_text())
+    return json.loads((GOLDEN / "line2d_full.json").read_text())
 
 
 def image_sha256(img) -> str:

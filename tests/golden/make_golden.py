@@ -14,7 +14,7 @@ Stored per fixture (``<name>.npz``):
     su_headers    [ntraces, 60] int32: the SU header words it wrote
     jobs          (jobs_x, jobs_y)
 
-Also ``config1_full.json``: the reference's image of the full config-1
+Also ``line2d_full.json``: the reference's image of the full 2-D
 line (synth.line2d(): 200 CMPs x 48 offsets, 1001 samples, 1.61e9 pairs,
 one rank), too large to store, recorded as the SHA-256 of its float32
 bytes ([traces][ns], little-endian, SU trace order) with its norm.
@@ -67,7 +67,7 @@ def run_reference(s, jx: int, jy: int, work: Path):
     return refbuild.read_image(work / "run", s.ns, jx * jy)
 
 
-def config1_full() -> dict:
+def line2d_full() -> dict:
     s = synth.line2d()
     with tempfile.TemporaryDirectory() as td:
         _, img = run_reference(s, 1, 1, Path(td))
@@ -80,8 +80,8 @@ def config1_full() -> dict:
 
 
 def main():
-    (HERE / "config1_full.json").write_text(json.dumps(config1_full(), indent=1) + "\n")
-    print("config1_full.json")
+    (HERE / "line2d_full.json").write_text(json.dumps(line2d_full(), indent=1) + "\n")
+    print("line2d_full.json")
     for name, (s, jx, jy) in fixtures().items():
         with tempfile.TemporaryDirectory() as td:
             hdr, img = run_reference(s, jx, jy, Path(td))

@@ -37,14 +37,14 @@ def test_golden_fixture(kpstm_lib, oracle_lib, name):
     assert np.max(np.abs(img - image)) <= 1e-5 * np.max(np.abs(image))
 
 
-def test_config1_full_size(kpstm_lib, oracle_lib):
+def test_full_line_size(kpstm_lib, oracle_lib):
     """200 CMPs x 48 offsets, ns=1001: 1.6 G pairs.  The restatement's image
     is the compiled reference's output byte for byte (its SHA-256 recorded by
     tests/golden/make_golden.py); the GPU's accumulators equal the
     restatement's bit for bit, and its finished image is within 1e-5 of the
     reference's."""
-    from fixtures import config1_golden, image_sha256
-    gold = config1_golden()
+    from fixtures import line2d_golden, image_sha256
+    gold = line2d_golden()
     s = synth.line2d()
     g = migrate(s, want_acc=True)
     o = oracle_lib.kirchhoff(s)

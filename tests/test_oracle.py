@@ -86,13 +86,13 @@ def test_oracle_matches_fresh_reference_runs(oracle_lib, seed):
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), rel_l2(got, ref)
 
 
-def test_restatement_is_the_reference_on_config1_full(oracle_lib):
-    """Config 1 at full size (200 CMPs x 48 offsets x 1001 samples, 1.61e9
+def test_restatement_is_the_reference_on_the_full_line(oracle_lib):
+    """The 2-D line at full size (200 CMPs x 48 offsets x 1001 samples, 1.61e9
     pairs): the C restatement's finished image has exactly the bytes of the
     compiled reference's own output (its SHA-256 recorded by
     tests/golden/make_golden.py)."""
-    from fixtures import config1_golden, image_sha256
-    gold = config1_golden()
+    from fixtures import line2d_golden, image_sha256
+    gold = line2d_golden()
     s = synth.line2d()
     o = oracle_lib.kirchhoff(s, want_acc=False)
     img = o["image"].reshape(-1, s.ns)
