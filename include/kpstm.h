@@ -345,6 +345,14 @@ int kpstm_debug_wait_limit(kpstm_ctx *ctx, uint32_t polls);
    out of memory (KPSTM_ERR_OUT_OF_MEMORY); -1 disarms.  Process-wide, one
    shot. */
 int kpstm_debug_fail_alloc(int32_t nth);
+/* The imaging kernel leaves out of an image tile's trace list, for one time
+   window, every trace whose traveltimes to all of the tile's columns lie
+   past the trace end at every sample of the window (a lower bound of the
+   double-square-root time with a relative margin of 2^-12, so that only
+   pairs the kernel would skip anyway are left out).  enable = 0 turns this
+   off, so that a test can show the images are bit-identical either way.
+   Per context; default on. */
+int kpstm_debug_trace_cull(kpstm_ctx *ctx, int32_t enable);
 
 /* ---- stand-alone set-up helpers (host only) -------------------------------- */
 

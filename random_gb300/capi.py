@@ -171,6 +171,7 @@ def load() -> C.CDLL:
     _sig(lib, "kpstm_velocity_from_segy", C.c_int, [_VOIDP, i64, i32, i32, i32, i32, i32, i32, _VOIDP, i64])
     _sig(lib, "kpstm_debug_wait_limit", C.c_int, [_VOIDP, C.c_uint32])
     _sig(lib, "kpstm_debug_fail_alloc", C.c_int, [C.c_int32])
+    _sig(lib, "kpstm_debug_trace_cull", C.c_int, [_VOIDP, C.c_int32])
     _sig(lib, "kpstm_strerror", C.c_char_p, [C.c_int])
     _sig(lib, "kpstm_abi_version", C.c_int, [])
     _lib = lib

@@ -107,6 +107,7 @@ struct kpstm_ctx {
     int nrow;                    /* velocity rows of the slab */
     int dbound_ok;
     uint32_t wait_polls;         /* imaging stage waits give up after this many polls */
+    int32_t cull;                /* the imaging kernel's dead-window trace cull */
     /* stream handling / profiling */
     cudaStream_t own_cs;
     int prof;
@@ -632,6 +633,7 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
     kpstm_ctx *c = (kpstm_ctx *)calloc(1, sizeof(kpstm_ctx));
     if (!c) return KPSTM_ERR_OUT_OF_MEMORY;
     c->wait_polls = KP_WAIT_POLLS;
+    c->cull = 1;
     c->p = *params;
     c->s = s;
     cudaGetDevice(&c->device);
@@ -680,8 +682,6 @@ extern "C" int kpstm_create(const kpstm_params *params, const kpstm_velocity *ve
         for (int t = 0; t < ns; ++t) {
             c4[t] = 4.0 * (double)t2[t];
             c4r[t] = t > 0 ? 1.0 / c4[t] : 0.0;
-            double t0 = (double)t * (double)params->dt;
-            (void)t0;
             /* full mode works in sample units: (t/2)^2 and t0/(8 dt^2) = t/(8 dt);
                t = 0 gets a tiny positive time so that rsqrt never sees 0 */
             t2c[t] = make_float2(t > 0 ? (float)(0.25 * (double)t * (double)t) : 1e-12f,
@@ -1161,6 +1161,15 @@ extern "C" int kpstm_debug_wait_limit(kpstm_ctx *c, uint32_t polls)
     return KPSTM_OK;
 }
 
+extern "C" int kpstm_debug_trace_cull(kpstm_ctx *c, int32_t enable)
+{
+    if (!c) return KPSTM_ERR_INVALID_ARG;
+    KP_CUDA(cudaStreamSynchronize(c->cs));
+    drop_graphs(c); /* captured launches hold the old setting */
+    c->cull = enable ? 1 : 0;
+    return KPSTM_OK;
+}
+
 extern "C" int kpstm_get_launch(const kpstm_ctx *c, kpstm_launch *cfg)
 {
     if (!c || !cfg) return KPSTM_ERR_INVALID_ARG;
@@ -1420,6 +1429,7 @@ static KpImageArgs image_args(const kpstm_ctx *c)
     a.aax = (float)p->iline_distance;
     a.aay = (float)p->xline_distance;
     a.wait_polls = c->wait_polls;
+    a.cull = c->cull;
     return a;
 }
 

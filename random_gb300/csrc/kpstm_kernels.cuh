@@ -84,6 +84,7 @@ struct KpImageArgs {
     int nitems;                    /* persistent mode: ntile * nwin * classes */
     const int32_t *cls_order;      /* persistent mode: classes, largest first */
     uint32_t wait_polls;           /* polls before a stage wait gives up (KP_WAIT_POLLS) */
+    int32_t cull;                  /* leave out traces dead over a tile's whole window */
 };
 
 /* ------------------------------------------------------------------------ */
@@ -380,12 +381,22 @@ __device__ __forceinline__ bool kp_tile_test(const float4 &box, float cx, float 
     return dx * dx + dy * dy < r2;
 }
 
+/* distance from (x, y) to the tile's box of column positions: at most the
+   distance to any of its columns */
+__device__ __forceinline__ float kp_box_dist(const float4 &box, float x, float y)
+{
+    const float dx = fmaxf(fmaxf(box.x - x, x - box.y), 0.0f);
+    const float dy = fmaxf(fmaxf(box.z - y, y - box.w), 0.0f);
+    return sqrtf(dx * dx + dy * dy);
+}
+
 /* Shared-memory layout of k_image: s_v (8 warps x W float2), s_t (W
-   float2), S one-trace TMA stages (kp_stages), the compaction list, then 26 ints
-   (8 warp counts, 8 stage counters, 8 last-issued sequence numbers, 2 flags)
-   ending right before the S mbarriers.  Returns the total bytes;
+   float2), S one-trace TMA stages (kp_stages), the compaction list, then 50
+   words (8 column positions, 8 critical distances, 8 warp counts, 8 stage
+   counters, 8 last-issued sequence numbers, 2 flags) ending right before the
+   S mbarriers.  Returns the total bytes;
    *bar_offset receives the barriers' offset (8-byte aligned). */
-#define KP_IMG_INTS 26
+#define KP_IMG_INTS 50
 /* TMA stages of the imaging kernel: 2 x the batch of the mode, or 2 for the
    three-CTAs-per-SM variant (MINB 3), whose shared memory must fit 3 times */
 __host__ __device__ constexpr int kp_stages(bool full, int minb)
@@ -443,20 +454,45 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
     int32_t *s_wsum = s_cnt - 8;                                             /* [8] */
     volatile int32_t *vflag = s_flag;
 
+    float *s_crit = reinterpret_cast<float *>(s_wsum) - 8;                   /* [8] */
+    float2 *s_col = reinterpret_cast<float2 *>(s_crit - 16);                 /* [8] column x, y (NaN: none) */
+
     __syncthreads(); /* the previous item of this CTA is done with shared memory */
     const int vrow = colok ? a.colrow[col] : -1;
     const float rdt2 = a.rdt * a.rdt;
+    /* the window's critical squared distance crit: every pair of this
+       column and window lies past the trace end for a trace whose source
+       and receiver distances dS, dR satisfy (dS + dR)^2 >= crit, because
+       sqrt(x + dS^2 y) + sqrt(x + dR^2 y) >= sqrt(4 x + (dS + dR)^2 y)
+       (Minkowski).  Full mode, in samples: x = tx, y = ty, crit = max of
+       (T^2 - 4 tx) / ty with T = (ns - 1)(1 + 2^-12) (Tf >= ns - 1 skips);
+       reference mode, in seconds: x = t2, y = 1 / v2, crit = max of
+       (T^2 - 4 t2) v2 with T = ns dt (1 + 2^-12) (RN(S/dt) >= ns skips).
+       The margin covers every rounding and the SFU square roots.  +inf
+       (no culling) where the column has no velocity row, so that the
+       velocity-range error is still raised; fmaxf drops NaN (a NaN y makes
+       every pair of its sample dead) */
+    float crit = colok ? (vrow < 0 ? INFINITY : -INFINITY) : -INFINITY;
     if (FULL) {
+        const float T = (a.nsf - 1.0f) * (1.0f + 1.0f / 4096.0f);
+        const float T2 = T * T;
         for (int i = lane; i < (K / 2) * 32; i += 32) {
             const int q = i >> 5, l = i & 31;
             const int ta = tw0 + l + 64 * q, tb = ta + 32;
             float2 va = make_float2(1.0f, 1.0f), vb = make_float2(1.0f, 1.0f);
             if (vrow >= 0 && ta < ns) va = a.vrows[(int64_t)vrow * ns + ta];
             if (vrow >= 0 && tb < ns) vb = a.vrows[(int64_t)vrow * ns + tb];
-            reinterpret_cast<float4 *>(s_v)[(w * (K / 2) + q) * 32 + l] =
+            const float4 e =
                 make_float4(ta < ns ? a.t2c[ta].x : 1.0f, tb < ns ? a.t2c[tb].x : 1.0f, va.y * rdt2, vb.y * rdt2);
+            reinterpret_cast<float4 *>(s_v)[(w * (K / 2) + q) * 32 + l] = e;
+            if (vrow >= 0) {
+                if (ta < ns) crit = fmaxf(crit, __fdiv_rn(__fsub_rn(T2, 4.0f * e.x), e.z));
+                if (tb < ns) crit = fmaxf(crit, __fdiv_rn(__fsub_rn(T2, 4.0f * e.y), e.w));
+            }
         }
     } else {
+        const float T = a.nsf * a.dt * (1.0f + 1.0f / 4096.0f);
+        const float T2 = T * T;
         for (int i = lane; i < (K / 2) * 32; i += 32) {
             const int q = i >> 5, l = i & 31;
             const int ta = tw0 + l + 64 * q, tb = ta + 32;
@@ -464,14 +500,22 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
             if (vrow >= 0 && ta < ns) va = a.vrows[(int64_t)vrow * ns + ta];
             if (vrow >= 0 && tb < ns) vb = a.vrows[(int64_t)vrow * ns + tb];
             reinterpret_cast<float4 *>(s_v)[(w * (K / 2) + q) * 32 + l] = make_float4(va.x, vb.x, -va.y, -vb.y);
+            if (vrow >= 0) {
+                if (ta < ns) crit = fmaxf(crit, __fmul_rn(__fsub_rn(T2, 4.0f * a.t2[ta]), va.x));
+                if (tb < ns) crit = fmaxf(crit, __fmul_rn(__fsub_rn(T2, 4.0f * a.t2[tb]), vb.x));
+            }
         }
         for (int i = tid; i < (K / 2) * 32; i += KP_THREADS) {
             const int ta = tw0 + (i & 31) + 64 * (i >> 5), tb = ta + 32;
             reinterpret_cast<float2 *>(s_t)[i] = make_float2(ta < ns ? a.t2[ta] : 0.0f, tb < ns ? a.t2[tb] : 0.0f);
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) crit = fmaxf(crit, __shfl_xor_sync(0xffffffffu, crit, o));
+    if (lane == 0) s_crit[w] = crit;
     const float2 cxy = colok ? a.colxy[col] : make_float2(0.f, 0.f);
     const float IX = cxy.x, IY = cxy.y;
+    if (lane == 0) s_col[w] = colok ? cxy : make_float2(NAN, NAN);
     const float4 box = a.tilebox[tile];
     const int64_t obase = ((int64_t)cls * a.ncol + (colok ? col : 0)) * ns + tw0 + lane;
 
@@ -507,20 +551,40 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
 
     const int cb = a.class_start[cls], ce = a.class_start[cls + 1];
     const uint32_t row_bytes = (uint32_t)(row * sizeof(float));
-    int my_hits = 0;
+    int my_hits = 0, cull_hits = 0;
     bool abort = false;
     const float tmax = a.nsf - 1.0f;
 
     for (int c0 = cb; c0 < ce && !abort; c0 += KP_LCH) {
         /* order-preserving compaction of the chunk's traces that can reach
-           any column of this tile */
+           any column of this tile and whose traveltimes can fall inside the
+           trace somewhere in the window */
         int n = 0;
+        float crit2 = -INFINITY; /* the tile's critical squared distance */
+#pragma unroll
+        for (int v = 0; v < 8; ++v) crit2 = fmaxf(crit2, s_crit[v]);
         for (int r = 0; r < KP_LCH / KP_THREADS; ++r) {
             int i = c0 + r * KP_THREADS + tid;
             bool pass = false;
             if (i < ce) {
                 const kpstm_geom &g = a.geom[i];
                 pass = kp_tile_test(box, g.cmpx, g.cmpy, a.tile_r2);
+                if (pass && a.cull) {
+                    const float D = kp_box_dist(box, g.sxt, g.syt) + kp_box_dist(box, g.gxt, g.gyt);
+                    if (D * D >= crit2) {
+                        pass = false;
+                        /* the pair count takes every (trace, column) in aperture
+                           (Kirchhoff.c:1352-1354): window 0 counts the culled
+                           trace's columns with the warps' own test */
+                        if (win == 0)
+#pragma unroll
+                            for (int v = 0; v < 8; ++v) {
+                                const float2 c = s_col[v];
+                                const float ex = __fsub_rn(c.x, g.cmpx), ey = __fsub_rn(c.y, g.cmpy);
+                                cull_hits += __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)) < a.aperture_x2;
+                            }
+                    }
+                }
             }
             unsigned m = __ballot_sync(0xffffffffu, pass);
             if (lane == 0) s_wsum[w] = __popc(m);
@@ -785,7 +849,10 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
         }
     }
     flush_counts();
-    if (win == 0 && lane == 0 && my_hits) atomicAdd(a.hits, (unsigned long long)my_hits);
+    if (win == 0) {
+        const int h = __reduce_add_sync(0xffffffffu, cull_hits) + (lane == 0 ? my_hits : 0);
+        if (lane == 0 && h) atomicAdd(a.hits, (unsigned long long)h);
+    }
     return true;
 }
 

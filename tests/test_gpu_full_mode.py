@@ -13,7 +13,7 @@ import pytest
 
 from fixtures import rel_l2
 from random_gb300 import capi, synth
-from random_gb300.migration import migrate
+from random_gb300.migration import Migration, migrate
 
 pytestmark = pytest.mark.gpu
 ACC_TOL = 1e-4
@@ -103,3 +103,52 @@ def test_fold_counts_beyond_16_bits(kpstm_lib):
     b = migrate(s, block=3000, want_acc=True)
     assert int(a["fold"].max()) > 32_768
     assert np.array_equal(a["km"], b["km"]) and np.array_equal(a["fold"], b["fold"])
+
+
+def _dead_window_share(m, kw, window):
+    """Share of the (trace, in-aperture column, time window) visits whose
+    summed source and receiver distances D satisfy D^2 >= max over the
+    window of (T^2 - 4 tx) / ty: the float64 form of the kernel's cull
+    bound, per column (the kernel takes the tile's box and window)."""
+    ns, dt, b = kw["ns"], kw["dt"], kw["bin_m"]
+    p = m.survey.params
+    X, Y = np.meshgrid((p["start_iline"] + np.arange(kw["nx"])) * b, (p["start_xline"] + np.arange(kw["ny"])) * b,
+                       indexing="ij")
+    X, Y = X.ravel(), Y.ravel()
+    t = np.arange(ns)
+    v = synth.vrms_3d(X[:, None], (t * dt)[None, :], 1600.0, 500.0, 100.0, 8000.0)
+    T = (ns - 1) * (1.0 + 2.0 ** -12)
+    crit = (T * T - t[None, :] ** 2.0) * (v * dt) ** 2
+    sx, sy, gx, gy = m.coords.T
+    inap = ((X[None, :] - 0.5 * (sx + gx)[:, None]) ** 2 + (Y[None, :] - 0.5 * (sy + gy)[:, None]) ** 2
+            < kw["aperture"] ** 2)
+    D = (np.hypot(X[None, :] - sx[:, None], Y[None, :] - sy[:, None])
+         + np.hypot(X[None, :] - gx[:, None], Y[None, :] - gy[:, None]))
+    dead = sum((inap & (D * D >= crit[:, w0:w0 + window].max(1)[None, :])).sum() for w0 in range(0, ns, window))
+    return dead / (inap.sum() * len(range(0, ns, window)))
+
+
+@pytest.mark.parametrize("mode,K", [(capi.MODE_FULL, 8), (capi.MODE_FULL, 16), (capi.MODE_REFERENCE, 8),
+                                    (capi.MODE_REFERENCE, 32)])
+def test_dead_window_cull_is_invisible(kpstm_lib, mode, K):
+    """The imaging kernel leaves out of a tile's trace list, per time
+    window, the traces whose traveltimes lie past the trace end at every
+    sample of the window, by sqrt(x + dS^2 y) + sqrt(x + dR^2 y) >=
+    sqrt(4 x + (dS + dR)^2 y) with a 2^-12 margin.  Far offsets against
+    short traces: over a tenth of the visits are dead; accumulators, fold
+    counts and the pair count are identical with the cull turned off."""
+    kw = dict(ntr=500, ns=401, dt=0.004, nx=12, ny=10, bin_m=25.0, max_offset=3500.0, n_refl=3, n_diff=10,
+              freq=25.0, aperture=1500.0, aa_cutoff=60.0, seed=23, mode=mode, output=capi.OUT_STACK)
+    assert _dead_window_share(synth.patch3d_model(**kw), kw, 32 * K) > 0.1
+    s = synth.patch3d(**kw)
+    out = []
+    for cull in (1, 0):
+        with Migration(s.params, s.velocity) as m:
+            m.set_launch(samples_per_lane=K)
+            assert kpstm_lib.kpstm_debug_trace_cull(m._h, cull) == 0
+            m.add_traces(s.headers, s.samples)
+            out.append((*m.accumulators(), m.pairs()))
+    assert out[0][1].max() > 0
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
