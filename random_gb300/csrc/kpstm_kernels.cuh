@@ -16,6 +16,8 @@
 #ifndef KPSTM_KERNELS_CUH
 #define KPSTM_KERNELS_CUH
 
+#include <type_traits>
+
 #include "kpstm_device.cuh"
 
 #define KP_TB_REF 4     /* traces per staged batch, reference mode */
@@ -760,7 +762,13 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                             const float2 rr2 = make_float2(kp_rsqrt_approx(ar2.x), kp_rsqrt_approx(ar2.y));
                             const float2 Tf2 = __ffma2_rn(as2, rs2, __fmul2_rn(ar2, rr2));
                             const bool va = Tf2.x < tmax, vb = Tf2.y < tmax; /* late samples of far traces skip */
-                            if (va && vb) {
+                            /* both halves through the packed arithmetic.  MASKED: a half
+                               past the trace end reads the table at Tf = 0 (inside it:
+                               floor(-Lf) >= -lmax >= 1 - tm) and adds exactly 0 (weight and
+                               tap both set to 0, so that no NaN of the table reaches it) */
+                            auto packed = [&](auto masked_t) {
+                                constexpr bool MASKED = decltype(masked_t)::value;
+                                const float2 Tp = MASKED ? make_float2(va ? Tf2.x : 0.0f, vb ? Tf2.y : 0.0f) : Tf2;
                                 const float2 gxx = __ffma2_rn(kp_bc2(axs), rs2, __fmul2_rn(kp_bc2(axr), rr2));
                                 const float2 gyy = __ffma2_rn(kp_bc2(ays), rs2, __fmul2_rn(kp_bc2(ayr), rr2));
                                 const float2 sg = make_float2(__fadd_rn(fabsf(gxx.x), fabsf(gyy.x)),
@@ -769,29 +777,42 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 Lf2 = make_float2(fminf(Lf2.x, a.lmaxf), fminf(Lf2.y, a.lmaxf));
                                 const float2 ui = __fmul2_rn(__fadd2_rn(rs2, rr2),
                                                              make_float2(kp_rcp_approx(Lf2.x), kp_rcp_approx(Lf2.y)));
-                                const float2 w2 = __fmul2_rn(ui, ui);
-                                const float2 ya2 = __fadd2_rn(Tf2, Lf2), yb2 = kp_sub2(Tf2, Lf2);
+                                float2 w2 = __fmul2_rn(ui, ui);
+                                const float2 ya2 = __fadd2_rn(Tp, Lf2), yb2 = kp_sub2(Tp, Lf2);
                                 const float2 mg = kp_bc2(KP_MAGIC);
-                                const float2 B0 = __fadd2_rz(Tf2, mg), Ba = __fadd2_rz(ya2, mg), Bb = __fadd2_rz(yb2, mg);
+                                const float2 B0 = __fadd2_rz(Tp, mg), Ba = __fadd2_rz(ya2, mg), Bb = __fadd2_rz(yb2, mg);
                                 /* fractions y - floor(y), with M - B = -floor(y) exactly */
                                 const float2 fa = __fadd2_rn(ya2, kp_sub2(mg, Ba));
                                 const float2 fb = __fadd2_rn(yb2, kp_sub2(mg, Bb));
                                 /* -2 f0 = 2 floor(Tf) - 2 Tf: 2 B0 - 2M is exact, and so is
                                    -2 (Tf - floor(Tf)) for Tf >= 0 (one rounding of an exact value) */
-                                const float2 m2f0 = __ffma2_rn(Tf2, kp_bc2(-2.0f),
+                                const float2 m2f0 = __ffma2_rn(Tp, kp_bc2(-2.0f),
                                                                __ffma2_rn(B0, kp_bc2(2.0f), kp_bc2(-2.0f * KP_MAGIC)));
-                                const float2 tri2 = make_float2(
+                                float2 tri2 = make_float2(
                                     tri_of(__float_as_int(B0.x), __float_as_int(Ba.x), __float_as_int(Bb.x), m2f0.x, fa.x, fb.x),
                                     tri_of(__float_as_int(B0.y), __float_as_int(Ba.y), __float_as_int(Bb.y), m2f0.y, fa.y, fb.y));
+                                if (MASKED) {
+                                    w2 = make_float2(va ? w2.x : 0.0f, vb ? w2.y : 0.0f);
+                                    tri2 = make_float2(va ? tri2.x : 0.0f, vb ? tri2.y : 0.0f);
+                                }
                                 if (KAHAN) { /* comp = -c: y = w tri - c, -c' = y - (s - acc) */
                                     const float2 y = __ffma2_rn(w2, tri2, comp[q]);
                                     const float2 s2 = __fadd2_rn(acc[q], y);
                                     comp[q] = kp_sub2(y, kp_sub2(s2, acc[q]));
                                     acc[q] = s2;
                                 } else {
-                                    acc[q] = __ffma2_rn(w2, tri2, acc[q]);
+                                    acc[q] = __ffma2_rn(w2, tri2, acc[q]); /* + 0 for a masked half: exact */
                                 }
-                                cnt2[q] += 0x00010001u;
+                                cnt2[q] += MASKED ? ((uint32_t)va | ((uint32_t)vb << 16)) : 0x00010001u;
+                            };
+                            if (!KAHAN) {
+                                /* warp-uniform choice: a warp with a half past the trace end
+                                   takes the masked body once, not the packed and the scalar
+                                   one in turn (a Kahan update of 0 is no no-op: scalar there) */
+                                if (__all_sync(0xffffffffu, va && vb)) packed(std::false_type{});
+                                else if (__any_sync(0xffffffffu, va || vb)) packed(std::true_type{});
+                            } else if (va && vb) {
+                                packed(std::false_type{});
                             } else {
                                 float &cx = comp[KAHAN ? q : 0].x, &cy = comp[KAHAN ? q : 0].y;
                                 if (va) {
