@@ -952,7 +952,7 @@ struct KpDemigArgs {
 };
 
 #define KP_DM_WARPS 4  /* traces (warps) per demigration CTA */
-#define KP_DM_UNROLL 4 /* 32-sample groups per load batch */
+#define KP_DM_UNROLL 3 /* sample stride of the lanes = samples per lane per load batch (odd) */
 
 /* 1/(v dt)^2 per velocity-row sample, computed as k_image does it. */
 __global__ void k_rvdt(const float2 *vrows, int64_t n, float rdt2, float *out)
@@ -1159,19 +1159,24 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
             const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
             const float *m = bound ? nullptr : a.model + ((int64_t)col * a.ncls + cls) * ns;
             const float *vr = a.rvdt + (int64_t)vrow * ns;
-            /* 4 x 32 samples per step; their model and velocity loads (non-coherent,
-               so they can move ahead of the atomics) are all issued first */
+            /* 3 x 32 samples per step, lane l taking t0 + 3 l + u: one warp
+               instruction's entries then span three times as many rows where
+               the traveltime is flat in t (same-address atomics serialise), and
+               an odd stride keeps steep runs on distinct banks.  The integer
+               sums do not depend on the order.  The model and velocity loads
+               (non-coherent, so they can move ahead of the atomics) are all
+               issued first. */
             for (int t0 = 0; t0 < ns; t0 += 32 * KP_DM_UNROLL) {
                 float mv[KP_DM_UNROLL], rv[KP_DM_UNROLL];
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
-                    const int t = t0 + 32 * u + lane;
+                    const int t = t0 + KP_DM_UNROLL * lane + u;
                     mv[u] = t < ns ? (bound ? 1.0f : __ldg(m + t)) : 0.0f;
                     rv[u] = t < ns ? __ldg(vr + t) : 1.0f;
                 }
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
-                    const int t = t0 + 32 * u + lane, tt = min(t, ns - 1);
+                    const int t = t0 + KP_DM_UNROLL * lane + u, tt = min(t, ns - 1);
                     const float2 tv = make_float2(s_t2[tt], rv[u]); /* as k_image's s_v */
                     float rs, rr;
                     const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
