@@ -98,7 +98,7 @@ struct kpstm_ctx {
     float *d_ltable, *d_lkm, *d_lkc;
     unsigned long long *d_lhits;
     double *d_dotpart, *d_dot;
-    unsigned int *d_absmax;      /* demigration: bits of max |model| */
+    unsigned int *d_absmax;      /* demigration: bits of max |model|, then the 64-bit nonzero count */
     float *d_dbound;             /* demigration: per live trace max_k (L 1)[k] */
     float *d_wbound;             /* demigration: per live trace largest pair weight x t/(8 dt) */
     unsigned long long *d_dacc;  /* demigration: [nlive][ng] fixed-point trace accumulators */
@@ -1551,6 +1551,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     }
     if (a.limb_r > 21) a.limb_r = 21;
     a.absmax = c->d_absmax;
+    a.nmodel = (int64_t)s->nclass * s->ncol * ns;
     a.order = c->d_dorder;
     /* accumulator rows in shared memory when four of them fit with room for
        several CTAs per SM (and the radix leaves the limbs room), else in L2 */
@@ -1595,7 +1596,7 @@ static int lsm_forward_impl(kpstm_ctx *c, const float *d_model, float *d_data)
     a.dbound = c->d_dbound;
     a.wbound = c->d_wbound;
     const int64_t nmodel = (int64_t)s->nclass * s->ncol * ns;
-    KP_CUDA(cudaMemsetAsync(c->d_absmax, 0, sizeof(unsigned int), c->cs));
+    KP_CUDA(cudaMemsetAsync(c->d_absmax, 0, 2 * sizeof(unsigned long long), c->cs));
     k_absmax<<<4 * c->nsm, 256, 0, c->cs>>>(d_model, nmodel, c->d_absmax);
     KP_CUDA(cudaGetLastError());
     dm<<<nblk, 32 * KP_DM_WARPS, smem, c->cs>>>(a);
@@ -1736,7 +1737,7 @@ extern "C" int kpstm_lsm_geometry(kpstm_ctx *c, const int32_t *hdr_be, int64_t n
         }
         KP_LALLOC(c->d_dotpart, sizeof(double) * KP_DOT_BLOCKS);
         KP_LALLOC(c->d_dot, sizeof(double) * 4);
-        KP_LALLOC(c->d_absmax, sizeof(unsigned int));
+        KP_LALLOC(c->d_absmax, 2 * sizeof(unsigned long long));
         KP_LALLOC(c->d_dbound, sizeof(float) * (size_t)ntr);
         KP_LALLOC(c->d_wbound, sizeof(float) * (size_t)ntr);
         if (c->p.precision == KPSTM_PREC_BF16_KAHAN) KP_LALLOC(c->d_lkc, sizeof(float) * nimg);

@@ -930,7 +930,8 @@ struct KpDemigArgs {
     const int32_t *colrow;
     const float *rvdt;             /* [nrow][ns] RN(RN(1/v^2) / dt^2): k_image's 1/(v dt)^2 */
     const float2 *t2c;             /* [ns] {(t/2)^2, .} */
-    const unsigned int *absmax;    /* bits of max |model| (k_absmax) */
+    const unsigned int *absmax;    /* bits of max |model|, then (at +8 bytes) the nonzero count (k_absmax) */
+    int64_t nmodel;                /* model samples */
     const float *dbound;           /* [nlive] max_k (L 1)[trace, k] (bound pass), or null */
     const int32_t *order;          /* [nlive] visiting order of the live slots, or null */
     float *dbound_out;             /* bound pass: receives dbound */
@@ -952,7 +953,7 @@ struct KpDemigArgs {
 };
 
 #define KP_DM_WARPS 4  /* traces (warps) per demigration CTA */
-#define KP_DM_UNROLL 3 /* sample stride of the lanes = samples per lane per load batch (odd) */
+#define KP_DM_UNROLL 3 /* samples per lane per load batch; the lane stride of dense models (odd) */
 
 /* 1/(v dt)^2 per velocity-row sample, computed as k_image does it. */
 __global__ void k_rvdt(const float2 *vrows, int64_t n, float rdt2, float *out)
@@ -962,16 +963,22 @@ __global__ void k_rvdt(const float2 *vrows, int64_t n, float rdt2, float *out)
 }
 
 /* Largest |x| as float bits (the order of non-negative floats is that of
-   their bits); NaN counts as infinity. */
+   their bits; NaN counts as infinity) into out[0], and the count of nonzero
+   samples into the 64-bit word at out + 2. */
 __global__ void __launch_bounds__(256) k_absmax(const float *x, int64_t n, unsigned int *out)
 {
-    unsigned int m = 0;
+    unsigned int m = 0, nz = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float v = fabsf(x[i]);
         m = max(m, v == v ? __float_as_uint(v) : 0x7f800000u);
+        nz += v != 0.0f;
     }
     m = __reduce_max_sync(0xffffffffu, m);
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+    nz = __reduce_add_sync(0xffffffffu, nz);
+    if ((threadIdx.x & 31) == 0) {
+        if (m) atomicMax(out, m);
+        if (nz) atomicAdd(reinterpret_cast<unsigned long long *>(out + 2), (unsigned long long)nz);
+    }
 }
 
 /* Fire-and-forget 64-bit add in global memory (RED: no value comes back, so
@@ -1113,6 +1120,10 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
 
     const kpstm_geom g = a.geom[slot];
     const int cls = g.cls;
+    /* lane mapping: strided for models at least half nonzero (and the all-ones bound pass) */
+    const bool dense = bound || 2ull * reinterpret_cast<const unsigned long long *>(a.absmax)[1] >=
+                                    (unsigned long long)a.nmodel;
+    const int l0 = dense ? KP_DM_UNROLL * lane : lane, ls = dense ? 1 : 32;
     unsigned long long *Gg = SH ? nullptr : a.acc + (int64_t)slot * ng;
     const float apm = (float)a.aperture * 1.00001f + 1.0f; /* range margin; exact test below */
     const int x_lo = max(0, (int)floorf((g.cmpx - apm - a.ax0) / a.adx) - 1);
@@ -1159,24 +1170,26 @@ __global__ void __launch_bounds__(32 * KP_DM_WARPS, SH ? 7 : 8) k_demig(KpDemigA
             const float ays = __fmul_rn(sy, a.aay), ayr = __fmul_rn(gy, a.aay);
             const float *m = bound ? nullptr : a.model + ((int64_t)col * a.ncls + cls) * ns;
             const float *vr = a.rvdt + (int64_t)vrow * ns;
-            /* 3 x 32 samples per step, lane l taking t0 + 3 l + u: one warp
-               instruction's entries then span three times as many rows where
-               the traveltime is flat in t (same-address atomics serialise), and
-               an odd stride keeps steep runs on distinct banks.  The integer
-               sums do not depend on the order.  The model and velocity loads
-               (non-coherent, so they can move ahead of the atomics) are all
-               issued first. */
+            /* 3 x 32 samples per step.  Dense models: lane l takes t0 + 3 l + u,
+               so that one warp instruction's entries span three times as many
+               rows where the traveltime is flat in t (same-address atomics
+               serialise) while an odd stride keeps steep runs on distinct
+               banks.  Sparse models: lane l takes t0 + 32 u + l, so that the
+               clustered nonzero samples leave more warp instructions with
+               nothing to do (they skip).  The integer sums do not depend on
+               the order.  The model and velocity loads (non-coherent, so they
+               can move ahead of the atomics) are all issued first. */
             for (int t0 = 0; t0 < ns; t0 += 32 * KP_DM_UNROLL) {
                 float mv[KP_DM_UNROLL], rv[KP_DM_UNROLL];
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
-                    const int t = t0 + KP_DM_UNROLL * lane + u;
+                    const int t = t0 + l0 + ls * u;
                     mv[u] = t < ns ? (bound ? 1.0f : __ldg(m + t)) : 0.0f;
                     rv[u] = t < ns ? __ldg(vr + t) : 1.0f;
                 }
 #pragma unroll
                 for (int u = 0; u < KP_DM_UNROLL; ++u) {
-                    const int t = t0 + KP_DM_UNROLL * lane + u, tt = min(t, ns - 1);
+                    const int t = t0 + l0 + ls * u, tt = min(t, ns - 1);
                     const float2 tv = make_float2(s_t2[tt], rv[u]); /* as k_image's s_v */
                     float rs, rr;
                     const float Tf = kp_pair_time(dIS2, dIR2, tv, rs, rr);
