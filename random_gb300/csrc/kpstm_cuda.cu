@@ -6,7 +6,7 @@
  * the device (copy stream) while block b is imaged (compute stream), using
  * two staging slots; the call returns once its own host buffers have been
  * read.  Per block the compute stream runs
- *     k_geometry -> k_bucket -> k_prep -> k_image
+ *     k_geometry -> k_bucket -> k_prep (k_prep_ref in reference mode) -> k_image
  * with no host synchronisation; kpstm_finish runs k_deriv -> k_lowpass.
  */
 #include <cuda_runtime.h>
@@ -341,6 +341,19 @@ static unsigned prep_threads(const kpstm_ctx *c, int64_t ntr)
     return (unsigned)(32 * w);
 }
 
+/* The tap tables of up to ntr traces: k_prep_ref (32 traces per CTA) in
+   reference mode, k_prep (a thread per trace) in the full and precision
+   modes. */
+static void launch_prep(const kpstm_ctx *c, const KpPrepArgs &pa, int64_t ntr)
+{
+    if (!pa.full && !pa.exact) {
+        k_prep_ref<<<(unsigned)((ntr + KP_PR_TR - 1) / KP_PR_TR), 32 * KP_PR_WARPS, 0, c->cs>>>(pa);
+    } else {
+        const unsigned ptb = prep_threads(c, ntr);
+        k_prep<<<(unsigned)((ntr + ptb - 1) / ptb), ptb, 0, c->cs>>>(pa);
+    }
+}
+
 /* default patch: the fewest tiles (fewest idle warps), ties to the 4 x 2
    patch, then 2 x 4, 8 x 1, 1 x 8 (4 x 2 measured fastest on the 3-D survey) */
 static int default_px(const kpstm_setup *s)
@@ -553,8 +566,7 @@ static int enqueue_block(kpstm_ctx *c, const int32_t *d_hdr, const float *d_smp,
     pa.tm = s->dims.trange_max;
     pa.full = p->mode == KPSTM_MODE_FULL;
     pa.dt = p->dt;
-    const unsigned ptb = prep_threads(c, ntr);
-    k_prep<<<(unsigned)((ntr + ptb - 1) / ptb), ptb, 0, c->cs>>>(pa);
+    launch_prep(c, pa, ntr);
     KP_CUDA(cudaGetLastError());
     prof_end(c, pe, 1, 3);
 
@@ -1461,8 +1473,7 @@ static int lsm_adjoint_impl(kpstm_ctx *c, const float *d_data, const uint16_t *d
         pa.full = 1;
         pa.hilo = 1;
         pa.dt = c->p.dt;
-        const unsigned ptb = prep_threads(c, c->lsm_nlive);
-        k_prep<<<(unsigned)((c->lsm_nlive + ptb - 1) / ptb), ptb, 0, c->cs>>>(pa);
+        launch_prep(c, pa, c->lsm_nlive);
         KP_CUDA(cudaGetLastError());
         KpImageArgs a = image_args(c);
         a.geom = c->d_lgeom;

@@ -226,20 +226,14 @@ __global__ void __launch_bounds__(1024) k_class_order(const int32_t *class_start
     }
 }
 
-/* Per-trace tap tables, one thread per trace.
-   Reference mode: the running integrals of Kirchhoff.c:1312-1328 in the
-   reference's order and precision - the first integral adds f[t]/(4*t2[t])
-   in double and stores float, the tail adds f[ns-1]/(dt*dt*t*t) in float
-   (the fast-math a/(b*c) form of :1320), the second integral is a float
-   running sum, the front is mirrored - and the taps
-   D[T] = -2P[T] + P[T-2] + P[T+2] summed in double (:1391-1392), plus a zero
-   sentinel D[ns].
+/* Per-trace tap tables of the full and precision modes, one thread per
+   trace (reference mode: k_prep_ref below).
    Full mode: the double running integral P of the unscaled trace (P = 0
    before the trace, f = 0 after it), accumulated in double-word floats and
    stored over [-tm, ns+tm-4] as pairs {P[i], P[i+1]-P[i]} for linear
-   interpolation (ns + 2tm - 3 entries per row).  Only the reference-mode
-   branch, whose steps the reference defines in double (Kirchhoff.c:1316),
-   uses FP64. */
+   interpolation (ns + 2tm - 3 entries per row).
+   Precision mode: the reference-mode taps from the same integrals in
+   double-word floats, rounded once.  No FP64. */
 __global__ void k_prep(KpPrepArgs a)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -310,37 +304,107 @@ __global__ void k_prep(KpPrepArgs a)
             }
         }
         row[ns] = 0.0f;
-        return;
     }
-    const float flast = KP_SAMPLE(ns - 1);
-    const float dt2 = __fmul_rn(a.dt, a.dt);
-    float p1 = KP_SAMPLE(0);
-    float p2 = p1;
-    /* ring of P2[t-4..t] for the taps (held as doubles: each float P2 value
-       is widened once, exactly); P2[1], P2[2] kept for the mirror */
-    double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0, r4 = (double)p2;
-    double m1 = 0.0, m2 = 0.0;
-    for (int t = 1; t < ns + 2; ++t) {
-        if (t < ns) {
-            double v = __dadd_rn((double)p1, kp_ddiv_rn((double)KP_SAMPLE(t), a.c4[t], a.c4r[t]));
-            p1 = __double2float_rn(v);
-        } else {
-            float tf = __int2float_rn(t);
-            p1 = __fadd_rn(p1, __fdiv_rn(flast, __fmul_rn(__fmul_rn(dt2, tf), tf)));
-        }
-        p2 = __fadd_rn(p2, p1);
-        r0 = r1; r1 = r2; r2 = r3; r3 = r4; r4 = (double)p2; /* r4 = P2[t] */
-        if (t == 1) m1 = r4;
-        if (t == 2) m2 = r4;
-        if (t >= 2) {
-            int T = t - 2;
-            double pm = T >= 2 ? r0 : (T == 1 ? m1 : m2); /* P2[T-2], mirrored */
-            double d = __dadd_rn(__dadd_rn(-2.0 * r2, pm), r4);
-            if (T < ns) row[T] = __double2float_rn(d);
-        }
-    }
-    row[ns] = 0.0f; /* sentinel read for samples whose T >= ns */
 #undef KP_SAMPLE
+}
+
+/* Reference-mode tap tables: the running integrals of Kirchhoff.c:1312-1328
+   in the reference's order and precision - the first integral P1 adds
+   f[t]/(4 t2[t]) in double and stores float, the tail adds
+   f[ns-1]/(dt dt t t) in float (the fast-math a/(b c) form of :1320), the
+   second integral P2 is a float running sum, the front is mirrored - and
+   the taps D[T] = -2 P2[T] + P2[T-2] + P2[T+2] summed in double
+   (:1391-1392), plus a zero sentinel D[ns].  FP64 because the reference
+   defines these steps in double and parity needs them.
+   GB300 runs one FP64 warp instruction per ~64 cycles per sub-partition
+   whatever the active lanes, so a CTA takes 32 traces and the work is
+   split by what is sequential: per chunk of KP_PR_CH steps, all warps form
+   the 32 x CH double quotients (coalesced sample reads), warp 0 runs the 32
+   traces' running sums in lockstep (lane j = trace j: the only sequential
+   part, the same operations in the same order as a thread per trace), and
+   all warps form the taps from P2 in shared memory and store them
+   coalesced.  -2 P2[T] + P2[T-2] is one fma: the product is exact. */
+#define KP_PR_TR 32     /* traces per CTA */
+#define KP_PR_WARPS 8
+#define KP_PR_CH 64     /* steps per chunk */
+__global__ void __launch_bounds__(32 * KP_PR_WARPS) k_prep_ref(KpPrepArgs a)
+{
+    __shared__ double s_q[KP_PR_TR][KP_PR_CH + 1]; /* f[t] / (4 t2[t]), t = c0 + k */
+    __shared__ double s_p[KP_PR_TR][KP_PR_CH + 5]; /* P2[c0 - 4 + k] (widened, exact) */
+    __shared__ int32_t s_src[KP_PR_TR];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int ns = a.ns;
+    const int64_t base = blockIdx.x * (int64_t)KP_PR_TR;
+    const int64_t nl = *a.nlive;
+    if (base >= nl) return; /* block-uniform */
+    const int nh = (int)min((int64_t)KP_PR_TR, nl - base);
+    if (tid < KP_PR_TR) {
+        s_src[tid] = tid < nh ? a.order[base + tid] : 0;
+        if (tid < nh) {
+            const int64_t i = base + tid;
+            const kpstm_geom g = a.geom_raw[s_src[tid]];
+            a.geom[i] = g;
+            /* the row starts with the trace's geometry (staged with the taps) */
+            *reinterpret_cast<float4 *>(a.table + i * a.row) = make_float4(g.sxt, g.syt, g.gxt, g.gyt);
+            *reinterpret_cast<float4 *>(a.table + i * a.row + 4) =
+                make_float4(g.cmpx, g.cmpy, __int_as_float(g.cls), __int_as_float(g.src));
+            a.table[i * a.row + KP_ROW_HDR + ns] = 0.0f; /* sentinel read for samples whose T >= ns */
+        }
+    }
+    __syncthreads();
+    auto sample = [&](int j, int t) -> float {
+        const int64_t o = (int64_t)s_src[j] * ns + t;
+        return a.samples ? a.samples[o] : __fmul_rn(__uint_as_float(((uint32_t)a.samples_bf16[o]) << 16), a.scale[s_src[j]]);
+    };
+    float p1 = 0.0f, p2 = 0.0f; /* warp 0, lane j: trace j's running sums */
+    const float flast = (w == 0 && lane < nh) ? sample(lane, ns - 1) : 0.0f;
+    const float dt2 = __fmul_rn(a.dt, a.dt);
+    for (int c0 = 0; c0 < ns + 2; c0 += KP_PR_CH) {
+        const int cend = min(c0 + KP_PR_CH, ns + 2);
+        for (int idx = tid; idx < KP_PR_TR * KP_PR_CH; idx += 32 * KP_PR_WARPS) {
+            const int j = idx / KP_PR_CH, k = idx % KP_PR_CH, t = c0 + k;
+            if (j < nh && t >= 1 && t < ns) s_q[j][k] = kp_ddiv_rn((double)sample(j, t), a.c4[t], a.c4r[t]);
+        }
+        __syncthreads();
+        if (w == 0 && lane < nh) {
+            double *sp = s_p[lane];
+            const double *sq = s_q[lane];
+            int t = c0;
+            if (t == 0) {
+                p1 = sample(lane, 0);
+                p2 = p1;
+                sp[4] = (double)p2;
+                t = 1;
+            }
+            const int tq = min(cend, ns);
+            for (; t < tq; ++t) {
+                p1 = __double2float_rn(__dadd_rn((double)p1, sq[t - c0]));
+                p2 = __fadd_rn(p2, p1);
+                sp[4 + t - c0] = (double)p2;
+            }
+            for (; t < cend; ++t) { /* the two tail steps t = ns, ns + 1 */
+                const float tf = __int2float_rn(t);
+                p1 = __fadd_rn(p1, __fdiv_rn(flast, __fmul_rn(__fmul_rn(dt2, tf), tf)));
+                p2 = __fadd_rn(p2, p1);
+                sp[4 + t - c0] = (double)p2;
+            }
+        }
+        __syncthreads();
+        /* taps T whose last term P2[T + 2] is in this chunk: P2[x] sits at
+           s_p[j][4 + x - c0]; T = 0, 1 mirror the front (P2[2], P2[1]) */
+        for (int idx = tid; idx < KP_PR_TR * KP_PR_CH; idx += 32 * KP_PR_WARPS) {
+            const int j = idx / KP_PR_CH, T = c0 - 2 + idx % KP_PR_CH;
+            if (j >= nh || T < 0 || T >= ns || T >= cend - 2) continue;
+            const double *sp = s_p[j];
+            const double pm = T >= 2 ? sp[2 + T - c0] : sp[6 - T - c0];
+            const double d = __dadd_rn(__fma_rn(-2.0, sp[4 + T - c0], pm), sp[6 + T - c0]);
+            a.table[(base + j) * a.row + KP_ROW_HDR + T] = __double2float_rn(d);
+        }
+        __syncthreads();
+        if (cend == c0 + KP_PR_CH && tid < KP_PR_TR * 4) /* halo: P2[c0 + CH - 4 ..] */
+            s_p[tid >> 2][tid & 3] = s_p[tid >> 2][KP_PR_CH + (tid & 3)];
+        __syncthreads();
+    }
 }
 
 /* ------------------------------------------------------------------------ */
