@@ -794,31 +794,12 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 return fmaf(m2f0, Q0.y, ua + ub);
                             }
                         };
-                        /* one sample alone (its pair partner lies past the trace end) */
-                        auto tap1 = [&](float Tf, float rs, float rr, float rv2, float &wgt) -> float {
-                            float Lf;
-                            kp_pair_width(rs, rr, axs, axr, ays, ayr, rv2, a.lmaxf, Lf, wgt);
-                            const float ya = Tf + Lf, yb = Tf - Lf;
-                            const int b0 = kp_floor_bits(Tf), ba = kp_floor_bits(ya), bb = kp_floor_bits(yb);
-                            return tri_of(b0, ba, bb, -2.0f * (Tf - (__int_as_float(b0) - KP_MAGIC)),
-                                          ya - (__int_as_float(ba) - KP_MAGIC), yb - (__int_as_float(bb) - KP_MAGIC));
-                        };
-                        auto add1 = [&](float &ak, float &nck, float wgt, float tri) {
-                            if (KAHAN) { /* nck = -c */
-                                const float y = fmaf(wgt, tri, nck);
-                                const float s2 = ak + y;
-                                nck = y - (s2 - ak);
-                                ak = s2;
-                            } else {
-                                ak = fmaf(wgt, tri, ak);
-                            }
-                        };
 #pragma unroll
                         for (int q = 0; q < K / 2; ++q) {
                             /* samples t = tw0 + lane + 64q and t + 32 as one pair: the
                                packed operations round each half exactly as the scalar
-                               kp_pair_time / kp_pair_width do, so both paths (and the
-                               demigration) see identical pairs */
+                               kp_pair_time / kp_pair_width do, so that the demigration,
+                               which uses those, sees identical pairs */
                             const float4 vv = sv4[32 * q];
                             const float2 tx = make_float2(vv.x, vv.y), ty = make_float2(vv.z, vv.w);
                             const float2 as2 = __ffma2_rn(kp_bc2(dIS2), ty, tx), ar2 = __ffma2_rn(kp_bc2(dIR2), ty, tx);
@@ -828,8 +809,10 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                             const bool va = Tf2.x < tmax, vb = Tf2.y < tmax; /* late samples of far traces skip */
                             /* both halves through the packed arithmetic.  MASKED: a half
                                past the trace end reads the table at Tf = 0 (inside it:
-                               floor(-Lf) >= -lmax >= 1 - tm) and adds exactly 0 (weight and
-                               tap both set to 0, so that no NaN of the table reaches it) */
+                               floor(-Lf) >= -lmax >= 1 - tm) and leaves its sums as they
+                               were (plain sums add exactly 0: weight and tap both set to 0,
+                               so that no NaN of the table reaches them; Kahan sums keep
+                               their old value and compensation) */
                             auto packed = [&](auto masked_t) {
                                 constexpr bool MASKED = decltype(masked_t)::value;
                                 const float2 Tp = MASKED ? make_float2(va ? Tf2.x : 0.0f, vb ? Tf2.y : 0.0f) : Tf2;
@@ -862,36 +845,24 @@ __device__ __forceinline__ bool k_image_item(const KpImageArgs &a, uint8_t *smem
                                 if (KAHAN) { /* comp = -c: y = w tri - c, -c' = y - (s - acc) */
                                     const float2 y = __ffma2_rn(w2, tri2, comp[q]);
                                     const float2 s2 = __fadd2_rn(acc[q], y);
-                                    comp[q] = kp_sub2(y, kp_sub2(s2, acc[q]));
-                                    acc[q] = s2;
+                                    const float2 c2 = kp_sub2(y, kp_sub2(s2, acc[q]));
+                                    if (MASKED) {
+                                        comp[q] = make_float2(va ? c2.x : comp[q].x, vb ? c2.y : comp[q].y);
+                                        acc[q] = make_float2(va ? s2.x : acc[q].x, vb ? s2.y : acc[q].y);
+                                    } else {
+                                        comp[q] = c2;
+                                        acc[q] = s2;
+                                    }
                                 } else {
                                     acc[q] = __ffma2_rn(w2, tri2, acc[q]); /* + 0 for a masked half: exact */
                                 }
                                 cnt2[q] += MASKED ? ((uint32_t)va | ((uint32_t)vb << 16)) : 0x00010001u;
                             };
-                            if (!KAHAN) {
-                                /* warp-uniform choice: a warp with a half past the trace end
-                                   takes the masked body once, not the packed and the scalar
-                                   one in turn (a Kahan update of 0 is no no-op: scalar there) */
-                                if (__all_sync(0xffffffffu, va && vb)) packed(std::false_type{});
-                                else if (__any_sync(0xffffffffu, va || vb)) packed(std::true_type{});
-                            } else if (va && vb) {
-                                packed(std::false_type{});
-                            } else {
-                                float &cx = comp[KAHAN ? q : 0].x, &cy = comp[KAHAN ? q : 0].y;
-                                if (va) {
-                                    float wgt;
-                                    const float tri = tap1(Tf2.x, rs2.x, rr2.x, ty.x, wgt);
-                                    add1(acc[q].x, cx, wgt, tri);
-                                    cnt2[q] += 1u;
-                                }
-                                if (vb) {
-                                    float wgt;
-                                    const float tri = tap1(Tf2.y, rs2.y, rr2.y, ty.y, wgt);
-                                    add1(acc[q].y, cy, wgt, tri);
-                                    cnt2[q] += 0x00010000u;
-                                }
-                            }
+                            /* warp-uniform choice: a warp with a half past the trace end
+                               takes the masked body once, not the packed and a scalar one
+                               in turn */
+                            if (__all_sync(0xffffffffu, va && vb)) packed(std::false_type{});
+                            else if (__any_sync(0xffffffffu, va || vb)) packed(std::true_type{});
                         }
                     }
                 } while (0);
