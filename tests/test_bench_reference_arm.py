@@ -35,3 +35,20 @@ def test_reference_arm_prints_one_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_roofline_constants_of_the_committed_profiles():
+    """The ncu summaries that bench.py reads for its roofline sub-fields
+    parse, and hold every figure it uses; whether they match the current
+    kernel sources is reported per run in roofline.profile.stale."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    for name in sorted(set(bench.PROFILE_OF.values())):
+        pc = bench.profile_constants(name)
+        assert pc is not None, name
+        for key in ("kernel", "launch", "case", "source_sha256", "pairs", "warp_instructions", "issue_active",
+                    "xu_pipe", "dram_bytes", "lts_bytes", "lts_throughput", "duration_ns", "image_columns"):
+            assert key in pc, (name, key)
+        assert set(pc["launch"]) >= {"tile_px", "samples_per_lane", "persistent", "ctas_per_sm"}, name
+        assert pc["pairs"] > 0 and pc["warp_instructions"] > 0 and 0 < pc["issue_active"] <= 1, name
+        assert len(pc["source_sha256"]) == len(bench.kernel_source_hash()), name
