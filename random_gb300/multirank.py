@@ -78,6 +78,12 @@ def trace_shard(ntr: int, rank: int, world: int) -> slice:
     return slice(min(ntr, rank * per), min(ntr, (rank + 1) * per))
 
 
+def image_slab(nx: int, rank: int, world: int) -> slice:
+    """Contiguous block of inlines (image columns in x) of one rank: the
+    reference's slabs along x (Kirchhoff.c:280-300)."""
+    return trace_shard(nx, rank, world)
+
+
 def _allreduce(t):
     import torch.distributed as dist
     if dist.is_available() and dist.is_initialized():
@@ -124,6 +130,49 @@ def cgls_trace_shards(forward, adjoint, d_local, niter: int, store=None):
             break
         s = _allreduce(adjoint(r))
         gnew = float(torch.sum(s.double() * s.double()))
+        p = s.add_(p, alpha=gnew / gamma if gamma > 0 else 0.0)
+        gamma = gnew
+    return x, res
+
+
+def _local_dot(x, y) -> float:
+    """FP64 dot product of two replicated tensors (no exchange)."""
+    import torch
+    return float(torch.sum(x.double() * y.double()))
+
+
+def cgls_image_slabs(forward, adjoint, d, niter: int, store=None):
+    """CGLS on min |L m - d|^2 from m = 0 with the image cut into slabs across
+    the ranks (the reference's decomposition, Kirchhoff.c:280-300) and the
+    same recurrence as cgls_trace_shards.  Each rank holds its slab of every
+    model-space vector and the whole data space, replicated: forward(model
+    slab) -> that slab's contribution to every trace, summed over the ranks
+    by one data all-reduce per iteration; adjoint(data) -> its slab's image,
+    with no exchange.  Model-space dot products are summed by scalar
+    all-reduces, data-space ones are local, and every rank takes the same FP64
+    step lengths.  Returns (this rank's model slab, residual norms
+    [niter + 1])."""
+    import torch
+    store = store or (lambda v: v)
+    r = store(d.clone())
+    res = [_local_dot(r, r) ** 0.5]
+    s = adjoint(r)
+    x = torch.zeros_like(s)
+    if niter == 0:
+        return x, res
+    p = s.clone()
+    gamma = _dot(s, s)
+    for it in range(niter):
+        q = _allreduce(forward(p))
+        qq = _local_dot(q, q)
+        alpha = gamma / qq if qq > 0 else 0.0
+        x.add_(p, alpha=alpha)
+        r = store(r.sub_(q, alpha=alpha))
+        res.append(_local_dot(r, r) ** 0.5)
+        if it + 1 == niter:
+            break
+        s = adjoint(r)
+        gnew = _dot(s, s)
         p = s.add_(p, alpha=gnew / gamma if gamma > 0 else 0.0)
         gamma = gnew
     return x, res

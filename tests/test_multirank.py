@@ -140,3 +140,52 @@ def test_two_rank_trace_sharded_cgls_equals_one_rank(oracle_lib):
         assert np.allclose(res, res1, rtol=1e-12, atol=0)
         assert np.linalg.norm(x - x1[-1]) <= 1e-12 * np.linalg.norm(x1[-1])
     assert np.array_equal(out[0][1], out[1][1])  # the replicated model is the same on every rank
+
+
+def _slab_worker(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    from oracle import oracle
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        s = _lsm_survey()
+        d = _lsm_data(s)
+        sl = multirank.image_slab(6, rank, world)
+
+        def fwd(m_slab):
+            m = np.zeros((6, 5, 1, s.ns))
+            m[sl] = m_slab.numpy()
+            return torch.from_numpy(oracle.lsm_apply(s, 1, m))
+
+        adj = lambda r: torch.from_numpy(np.ascontiguousarray(oracle.lsm_apply(s, 0, r.numpy())[sl]))
+        x, res = multirank.cgls_image_slabs(fwd, adj, torch.from_numpy(d), 5)
+        q.put((rank, x.numpy(), res))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_image_slab_cgls_equals_one_rank(oracle_lib):
+    """Two gloo ranks, each with half the inlines of the image (the
+    reference's slabs) and the whole data, run CGLS with one data all-reduce
+    per iteration; their slabs put together are the single-rank FP64 CGLS
+    iterate (to summation-order rounding)."""
+    import torch.multiprocessing as mp
+    s = _lsm_survey()
+    x1, res1 = oracle_lib.cgls(s, _lsm_data(s), 5)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_slab_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted((q.get(timeout=300) for _ in procs), key=lambda o: o[0])
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for _, _, res in out:
+        assert np.allclose(res, res1, rtol=1e-12, atol=0)
+    x = np.concatenate([o[1] for o in out], axis=0)
+    assert x.shape == x1[-1].shape
+    assert np.linalg.norm(x - x1[-1]) <= 1e-12 * np.linalg.norm(x1[-1])
+
