@@ -20,7 +20,7 @@ one rank), too large to store, recorded as the SHA-256 of its float32
 bytes ([traces][ns], little-endian, SU trace order) with its norm.
 
 Run here (needs the reference checkout and gcc):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]
 """
 from __future__ import annotations
 
@@ -41,6 +41,23 @@ from random_gb300 import segy, synth  # noqa: E402
 HERE = Path(__file__).resolve().parent
 
 
+def _line_overhang_coarse_velocity():
+    """2-D line of 10 CMPs cut into 3 slabs of ceil(10/3) = 4 inlines, so that
+    the last slab runs 2 inlines past the end (Kirchhoff.c:266-300), with a
+    v_rms grid that covers them, varies along the line and is sampled at
+    twice the trace interval (the velocity sample of t is round(t dt / dtm),
+    Kirchhoff.c:1357-1378)."""
+    s = synth.line2d(n_cmp=10, n_off=4, ns=201, seed=8, aa_cutoff=40.0)
+    u = s.info["units_per_metre"]
+    v = s.velocity
+    nil, nsm, dtm = 12, 102, 2.0 * v.dtm
+    t0 = np.arange(nsm) * dtm
+    vt = ((1500.0 + 600.0 * t0[None, :] + 15.0 * np.arange(nil)[:, None]) * u).astype(np.float32)
+    s.velocity = synth.Velocity(n_iline=nil, n_xline=1, nsm=nsm, o_iline=v.o_iline, o_xline=v.o_xline,
+                                d_iline=1, d_xline=1, dtm=dtm, vrms=segy.ibm_roundtrip(vt[:, None, :].copy()))
+    return s
+
+
 def fixtures():
     """name -> (survey, jobs_x, jobs_y)"""
     return {
@@ -56,6 +73,9 @@ def fixtures():
                                            aperture=300.0, aa_cutoff=60.0, seed=7, mode=0,
                                            output=0, nh=4, oh=0.0, dh=200.0, rotate_deg=30.0,
                                            origin=(1000.0, 2000.0)), 2, 2),
+        # 2-D line, the last of 3 slabs past the end inline, coarse and
+        # laterally varying v_rms
+        "g4_line_overhang": (_line_overhang_coarse_velocity(), 3, 1),
     }
 
 
@@ -79,10 +99,14 @@ def line2d_full() -> dict:
             "max_abs": float(np.max(np.abs(img)))}
 
 
-def main():
-    (HERE / "line2d_full.json").write_text(json.dumps(line2d_full(), indent=1) + "\n")
-    print("line2d_full.json")
+def main(names=()):
+    """All fixtures, or only the named ones (``line2d_full`` for the JSON)."""
+    if not names or "line2d_full" in names:
+        (HERE / "line2d_full.json").write_text(json.dumps(line2d_full(), indent=1) + "\n")
+        print("line2d_full.json")
     for name, (s, jx, jy) in fixtures().items():
+        if names and name not in names:
+            continue
         with tempfile.TemporaryDirectory() as td:
             hdr, img = run_reference(s, jx, jy, Path(td))
         v = s.velocity
@@ -97,4 +121,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
