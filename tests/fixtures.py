@@ -9,7 +9,7 @@ import numpy as np
 from random_gb300 import segy, synth
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-NAMES = ["g1_line_oddns", "g2_line_slabs", "g3_patch_rotated", "g4_line_overhang"]
+NAMES = ["g1_line_oddns", "g2_line_slabs", "g3_patch_rotated", "g4_line_overhang", "g5_patch_xline_overhang"]
 
 
 def load(name: str):

@@ -76,6 +76,13 @@ def fixtures():
         # 2-D line, the last of 3 slabs past the end inline, coarse and
         # laterally varying v_rms
         "g4_line_overhang": (_line_overhang_coarse_velocity(), 3, 1),
+        # 3-D, 6 x 5 columns in 2 x 2 slabs: the second xline slab (3 of
+        # ceil(5/2)) runs one xline past the end (the v_rms grid is one
+        # xline wide, so it covers it); 3 offset classes, 40 Hz low-pass
+        "g5_patch_xline_overhang": (synth.patch3d(ntr=200, ns=180, dt=0.004, nx=6, ny=5, bin_m=25.0,
+                                                  max_offset=900.0, n_refl=2, n_diff=5, freq=25.0,
+                                                  aperture=400.0, aa_cutoff=40.0, seed=9, mode=0,
+                                                  output=0, nh=3, oh=0.0, dh=300.0), 2, 2),
     }
 
 
